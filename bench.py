@@ -1,0 +1,409 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 all-pairs n-body step (prints one JSON line on rank 0).
+
+Workload (default): one universe of N = 65536 bodies, positions U[-1000,1000]^3,
+velocities N(0,1), masses U[1,100] (seed 0), G = 6.6740831e-11, T = 1e3 -- FP32
+pairwise stage 1 with FP64 sums and FP64 stage 2 ("fp32" mode).  Synthetic data: the
+reference has no dataset, its own scenarios are generated too.
+
+  value      pair interactions per second (N^2 per step), device-timed steps with the
+             state resident in HBM; L2 flushed (256 MiB write) between timed steps
+  e2e        the same metric through the reference-facing plugin (gb1.universe.step()
+             with host_sync='full'): per step the FP64 r, v are uploaded from pinned
+             host memory and downloaded back, wall-clock timed
+  roofline   stage-1 kernel: 20 FLOP per interaction / kernel time, against the FP32
+             FMA peak measured live by grav_fp32_peak_probe (SMs x 128 x 2 x clock)
+  cpu_baseline  the reference's fastest CPU design (portable restatement in
+             oracle/ref_port.c: unique pairs, OpenMP, private accumulators) on the
+             host cores, on a bounded sample of the same workload
+
+--impl reference times that CPU implementation alone (rank 0; other ranks exit).
+Multi-GPU: the path runs one universe per GPU (replicas only, no collective);
+value = sum over ranks of interactions / the slowest rank's time.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ('pair-interactions/s/GPU at N=65536 and fwd+adjoint steps/s at ≤1e-5 FP64 err')
+UNIT = 'interactions/s'
+FLOP_PER_INTERACTION = 20
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', choices=('ours', 'reference'), default='ours')
+    ap.add_argument('--n', type=int, default=65536)
+    ap.add_argument('--mode', default='fp32', choices=('fp32', 'fp32c', 'fp64'))
+    ap.add_argument('--cpu-seconds', type=float, default=4.0,
+                    help='target seconds per CPU-baseline sample run (3 runs)')
+    ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--no-e2e', action='store_true')
+    a = ap.parse_args()
+    a.warmup = max(a.warmup, 3)
+    return a
+
+
+# ---- distributed plumbing ----------------------------------------------------------------
+
+def dist_env():
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return world, rank, local
+
+
+def dist_init(world, backend):
+    import torch.distributed as dist
+    if world > 1 and not dist.is_initialized():
+        os.environ.setdefault('MASTER_ADDR', '127.0.0.1')
+        dist.init_process_group(backend)
+    return dist
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(x, world, device):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---- clocks ---------------------------------------------------------------------------------
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clock and throttle reasons during the timed region."""
+    FIELDS = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+              'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+              'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix='.csv')
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.index), '--query-gpu=' + self.FIELDS,
+                 '--format=csv,noheader,nounits', '-lms', '200'],
+                stdout=open(self.path, 'w'), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, power, reasons = [], [], [], set()
+        names = ('hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap')
+        with open(self.path) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(',')]
+                if len(p) < 9:
+                    continue
+                try:
+                    sm.append(float(p[1]))
+                    smax.append(float(p[2]))
+                    power.append(float(p[3]))
+                except ValueError:
+                    continue
+                for nm, val in zip(names, p[5:9]):
+                    if val.lower() == 'active':
+                        reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['no samples']}
+        return {'sm_mhz': statistics.median(sm), 'sm_max_mhz': max(smax),
+                'power_w_max': max(power), 'samples': len(sm), 'reasons': sorted(reasons)}
+
+
+# ---- CPU baseline (the reference's CPU design, restated portably) -------------------------
+
+def cpu_baseline_run(n, seed, target_s, runs=3):
+    """Time the unique-pair OpenMP stage 1 (oracle/ref_port.c) on rows [0, k) of the pair
+    triangle of the workload, k sized for about target_s seconds; best of `runs`.
+    Returns (interactions/s, threads, sample description)."""
+    import oracle
+    from gravitation_gb300.scenarios import G_DEFAULT, uniform_cube
+    r, _, m = uniform_cube(n, seed=seed)
+    port = oracle.PortStage1(r, m, G_DEFAULT)
+    k0 = max(1, min(n, 256))
+    port.run(0, k0)  # first call starts the OpenMP thread team
+    t0 = time.perf_counter()
+    port.run(0, k0)
+    dt = time.perf_counter() - t0
+    rate = oracle.PortStage1.pairs_in_rows(n, 0, k0) / max(dt, 1e-6)
+    want = rate * target_s
+    k = k0
+    pairs = oracle.PortStage1.pairs_in_rows(n, 0, k)
+    while k < n and pairs < want:
+        step = max(1, min(n - k, int((want - pairs) / max(n - 1 - k, 1)) + 1))
+        pairs += sum(n - 1 - i for i in range(k, k + step))
+        k += step
+    best = None
+    for _ in range(runs):
+        t0 = time.perf_counter()
+        port.run(0, k)
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    value = 2.0 * pairs / best
+    sample = ('rows 0..%d of the unique-pair triangle of the N=%d workload (%d pairs = %d '
+              'interactions), FP32, best of %d runs of %.2f s' % (k, n, pairs, 2 * pairs, runs, best))
+    return value, port.threads, sample
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    value, threads, sample = cpu_baseline_run(args.n, 0, args.cpu_seconds, runs=args.steps)
+    line = {
+        'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': UNIT,
+        'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': 1e3 * args.n * args.n / value,
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+        'data': 'synthetic (seeded uniform cube)',
+        'config': {'workload': 'uniform cube N=%d seed 0, stage 1 FP32 (CPU)' % args.n,
+                   'n': args.n},
+        'cpu_baseline': {'value': value, 'unit': UNIT, 'cores': threads, 'kind': 'port',
+                         'sample': sample},
+        'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+        'note': ('oracle/ref_port.c restates the reference c4a design (unique pairs, OpenMP '
+                 'row segments balanced by pair count, private accumulators, serial '
+                 'reduction) portably; the reference c4a/c4b sources are x86 SSE only'),
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ---- ours --------------------------------------------------------------------------------------
+
+def measure_fp32_peak(torch, lib, info, device):
+    """FP32 FLOP/s of the FMA probe (best of 3 launches of ~20 ms)."""
+    import ctypes
+    blocks = info.sm_count * 8
+    out = torch.empty(blocks * 256, dtype=torch.float32, device=device)
+    s = torch.cuda.current_stream(device)
+    h = ctypes.c_void_p(s.cuda_stream)
+    iters = 2048
+    lib.grav_fp32_peak_probe(out.data_ptr(), blocks, 64, h)
+    best = None
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        lib.grav_fp32_peak_probe(out.data_ptr(), blocks, iters, h)
+        e1.record(s)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    fmas = blocks * 256 * iters * 8 * 16
+    return 2.0 * fmas / (best * 1e-3)
+
+
+def sampled_errors(eng, r, m, G, rows):
+    """Max relative error of the current forces on `rows` against the FP64 oracle,
+    on the FP32-rounded state (arithmetic) and on the FP64 state."""
+    import oracle
+    a = eng.forces().cpu().numpy()[rows]
+    r32 = r.astype(np.float32).astype(np.float64)
+    gm32 = (G * m).astype(np.float32).astype(np.float64)
+    e_arith = oracle.rel_err_per_body(a, oracle.accel_fp64(r32, gm32, 1.0, rows=rows,
+                                                           coincident=True)).max()
+    e_state = oracle.rel_err_per_body(a, oracle.accel_fp64(r, G * m, 1.0, rows=rows,
+                                                           coincident=True)).max()
+    return float(e_arith), float(e_state)
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    device = torch.device('cuda', local)
+    dist_init(world, 'nccl')
+    from gravitation_gb300 import _lib
+    from gravitation_gb300.engine import Engine, device_info
+    from gravitation_gb300.scenarios import G_DEFAULT, T_DEFAULT, uniform_cube
+    from gravitation_gb300.tune import default_tuner
+
+    lib = _lib.load()
+    info = device_info(local)
+    n = args.n
+    r, v, m = uniform_cube(n, seed=0)
+    gm = G_DEFAULT * m
+    eng = Engine([n], T_DEFAULT, mode=args.mode, tuner=default_tuner(), device=local)
+    eng.set_state(r, v, gm)
+    stream = torch.cuda.current_stream(device)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=device)
+
+    # accuracy on sampled bodies before timing (FP64 oracle on the host)
+    rows = np.random.default_rng(17).choice(n, 64, replace=False)
+    e_arith, e_state = (None, None)
+    if rank == 0:
+        e_arith, e_state = sampled_errors(eng, r, m, G_DEFAULT, rows)
+        eng.set_state(r, v, gm)
+
+    for _ in range(args.warmup):
+        eng.step(1)
+    torch.cuda.synchronize()
+    eng.raise_on_device_error()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    t_wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()
+        evs[k][0].record(stream)
+        eng.step(1)
+        evs[k][1].record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    t_wall = time.perf_counter() - t_wall0
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    eng.raise_on_device_error()
+
+    # stage-1 kernel alone (the dominant kernel) for the roofline
+    s1 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    for k in range(args.steps):
+        flush.zero_()
+        s1[k][0].record(stream)
+        eng.stage1()
+        s1[k][1].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    s1_ms = [a.elapsed_time(b) for a, b in s1]
+    peak = measure_fp32_peak(torch, lib, info, device)
+
+    total_ms = sum(step_ms)
+    my_ms = total_ms / args.steps
+    max_ms = allreduce_max(my_ms, world, device)
+    value = world * n * n / (max_ms * 1e-3)
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(args, r, v, m, local)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cv, threads, sample = cpu_baseline_run(n, 0, args.cpu_seconds)
+        cpu = {'value': cv, 'unit': UNIT, 'cores': threads, 'kind': 'port', 'sample': sample}
+
+    if rank != 0:
+        return 0
+    s1_avg = statistics.mean(s1_ms)
+    achieved = FLOP_PER_INTERACTION * n * n / (s1_avg * 1e-3)
+    traffic = read_profile_traffic()
+    line = {
+        'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world,
+        'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': max_ms,
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f32 pair terms, f64 sums and stage 2',
+        'data': 'synthetic (seeded uniform cube; the reference ships no dataset)',
+        'config': {'workload': 'one universe, N=%d uniform cube seed 0, G=%.8g, T=%g, %s '
+                               'stage 1 + FP64 stage 2' % (n, G_DEFAULT, T_DEFAULT, args.mode),
+                   'n': n, 'mode': args.mode,
+                   'tile': {'bpt': eng.tile.bpt, 'threads': eng.tile.threads,
+                            'jtile': eng.tile.jtile, 'grid': eng.info.grid},
+                   'l2': 'flushed between timed steps (256 MiB write)',
+                   'parallelism': 'replicas' if world > 1 else 'single GPU'},
+        'stage1_ms': s1_avg, 'step_ms_min': min(step_ms), 'wall_s_timed_region': t_wall,
+        'roofline': {'bound': 'fp32', 'achieved': achieved / 1e12, 'peak': peak / 1e12,
+                     'unit': 'TFLOP/s', 'frac': achieved / peak, 'traffic': traffic,
+                     'kernel': 'stage1_f32_kernel', 'flop_per_interaction': FLOP_PER_INTERACTION,
+                     'peak_kind': 'measured live (grav_fp32_peak_probe FFMA kernel)',
+                     'peak_formula_tflops_at_max_clock':
+                         info.sm_count * 128 * 2 * (clk.get('sm_max_mhz') or 2070) * 1e6 / 1e12},
+        'accuracy': {'max_rel_err_vs_fp64_oracle_on_fp32_positions': e_arith,
+                     'max_rel_err_vs_fp64_oracle_on_fp64_state': e_state,
+                     'bodies_sampled': int(len(rows))},
+        'clocks': clk,
+        'gpu_launches': 2 * args.steps,
+        'e2e': e2e,
+        'cpu_baseline': cpu,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_e2e(args, r, v, m, local):
+    """gb1.universe.step() timed by wall clock, FP64 r and v crossing PCIe/C2C each step."""
+    import torch
+    from gravitation_gb300.kernel import gb1
+    n = len(m)
+    u = gb1.universe(dtype='float32', precision=args.mode, host_sync='full', device=local)
+    for i in range(n):
+        u.add_object(name='s', r=[float(r[i, 0]), float(r[i, 1]), float(r[i, 2])],
+                     v=[float(v[i, 0]), float(v[i, 1]), float(v[i, 2])], m=float(m[i]))
+    u.start()
+    for _ in range(args.warmup):
+        u.step()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        u.step()
+        times.append(time.perf_counter() - t0)
+    u.stop()
+    mean = statistics.mean(times)
+    return {'value': n * n / mean, 'unit': UNIT, 'h2d_bytes_per_step': 2 * n * 32,
+            'd2h_bytes_per_step': 2 * n * 32, 'ms_per_step': 1e3 * mean,
+            'ms_per_step_min': 1e3 * min(times), 'path': 'gb1.universe.step(), host_sync=full'}
+
+
+def read_profile_traffic():
+    """DRAM bytes per stage-1 launch from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, 'profiles', 'stage1_fp32_n65536.md')
+    try:
+        with open(p) as f:
+            for line in f:
+                if line.startswith('dram_bytes_per_launch:'):
+                    return float(line.split(':', 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def main():
+    args = parse()
+    if args.impl == 'reference':
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == '__main__':
+    sys.exit(main())

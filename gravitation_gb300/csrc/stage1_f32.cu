@@ -1,0 +1,216 @@
+// stage1_f32.cu -- stage 1 (all-pairs accelerations) in the FP32 precision modes.
+//
+// Force law of the reference (np1.py:81-95, py1.py:57-64, pc2.py:75-89):
+//     a_i = sum_{j != i} G m_j (r_j - r_i) / |r_j - r_i|^3
+// evaluated as   d = r_j - r_i ;  r2 = |d|^2 + eps2 ;  w = Gm_j * rsqrt(r2)^3 ;  a += w d
+// with 12 FMA-pipe operations and one SFU reciprocal square root per interaction.
+// eps2 (grav_eps2) only keeps the zero-separation terms finite so that they vanish
+// with d = 0; it is absorbed by rounding for any separation the FP32 coordinates
+// resolve, so it is not a softening length.
+//
+// Work decomposition (persistent, "stream-K" over j-tiles): the plan lists every
+// (universe, i-tile) segment; each segment owns one work unit per j-tile of its
+// universe.  CTA c of G processes the contiguous unit range [c*U/G, (c+1)*U/G), so
+// every CTA gets the same number of j-tiles (+-1) whatever the universe sizes are.
+// Per segment a CTA holds B i-bodies per thread in registers, streams its j-tiles
+// through double-buffered shared memory with 1-D bulk copies (cp.async.bulk,
+// completion on an mbarrier), sums each j-tile's contribution in FP32 and folds
+// that partial into FP64 accumulators.  The FP64 partial of the CTA's piece of the
+// segment goes to its own slot of b.part; stage 2 adds the slots in a fixed order,
+// so results do not depend on scheduling.
+//
+// GRAV_MODE_FP32C reads a second FP32 array with the low parts of the positions
+// (x = hi + lo) and forms d = (hi_j - hi_i) + (lo_j - lo_i): the separation is then
+// accurate to FP32 relative precision however far the bodies are from the origin.
+#include "grav_device.cuh"
+
+namespace grav {
+
+template <int MODE, int B, int T, int J>
+__global__ void __launch_bounds__(T) stage1_f32_kernel(const grav_batch b)
+{
+	constexpr int NP = (MODE == GRAV_MODE_FP32C) ? 2 : 1;  // float4 arrays per body
+	constexpr int IT = B * T;                               // i-tile
+	constexpr uint32_t TILE_BYTES = J * sizeof(float4);
+	extern __shared__ __align__(128) float4 smem_tiles[];   // [2 buffers][NP][J]
+	__shared__ __align__(8) uint64_t bar[2];
+
+	const int tid = threadIdx.x;
+	const int64_t U = b.n_units;
+	const int64_t G = gridDim.x;
+	const int64_t c = blockIdx.x;
+	int64_t ub = c * U / G;
+	const int64_t ue = (c + 1) * U / G;
+	if (ub >= ue) return;  // uniform over the CTA
+
+	if (tid == 0) {
+		mbar_init(&bar[0], 1);
+		mbar_init(&bar[1], 1);
+		fence_barrier_init();
+	}
+	__syncthreads();
+
+	const float4* __restrict__ pos = static_cast<const float4*>(b.pos);
+	const float4* __restrict__ poslo = pos + b.n_pad_total;
+	const float eps2 = b.eps2;
+
+	// segment holding unit ub: the last segment whose unit_begin <= ub
+	int s;
+	{
+		int lo = 0, hi = b.n_seg - 1;
+		while (lo < hi) {
+			const int mid = (lo + hi + 1) >> 1;
+			if (b.seg[mid].unit_begin <= ub) lo = mid;
+			else hi = mid - 1;
+		}
+		s = lo;
+	}
+
+	uint32_t gt = 0;  // tiles consumed by this CTA so far (buffer gt&1, parity (gt>>1)&1)
+	bool timed_out = false;
+
+	while (ub < ue && s < b.n_seg) {
+		const grav_seg_desc S = b.seg[s];
+		if (S.n_units == 0 || S.unit_begin + S.n_units <= ub) {
+			++s;
+			continue;
+		}
+		const grav_univ_desc Uu = b.univ[S.u];
+		const int64_t jt0 = ub - S.unit_begin;
+		const int64_t jt1 = min(ue - S.unit_begin, (int64_t)S.n_units);
+		const int nt = static_cast<int>(jt1 - jt0);
+		const int64_t ibase = Uu.pad_off + S.il0;
+		const float4* __restrict__ jsrc = pos + Uu.pad_off;
+		const float4* __restrict__ jsrclo = poslo + Uu.pad_off;
+
+		// first j-tile of this piece; buffer gt&1 was last read two tiles ago and every
+		// thread has passed a barrier since
+		if (tid == 0) {
+			const int bs = gt & 1;
+			mbar_arrive_expect_tx(&bar[bs], NP * TILE_BYTES);
+			bulk_g2s(smem_tiles + (bs * NP) * J, jsrc + jt0 * J, TILE_BYTES, &bar[bs]);
+			if (NP == 2)
+				bulk_g2s(smem_tiles + (bs * NP + 1) * J, jsrclo + jt0 * J, TILE_BYTES, &bar[bs]);
+		}
+
+		float xi[B], yi[B], zi[B];
+		float xl[B], yl[B], zl[B];
+		float fx[B], fy[B], fz[B];
+		double ax[B], ay[B], az[B];
+#pragma unroll
+		for (int k = 0; k < B; ++k) {
+			const float4 p = pos[ibase + tid + k * T];
+			xi[k] = p.x;
+			yi[k] = p.y;
+			zi[k] = p.z;
+			if (NP == 2) {
+				const float4 q = poslo[ibase + tid + k * T];
+				xl[k] = q.x;
+				yl[k] = q.y;
+				zl[k] = q.z;
+			} else {
+				xl[k] = yl[k] = zl[k] = 0.f;
+			}
+			fx[k] = fy[k] = fz[k] = 0.f;
+			ax[k] = ay[k] = az[k] = 0.0;
+		}
+
+		for (int t = 0; t < nt; ++t, ++gt) {
+			const int bs = gt & 1;
+			const bool ok = mbar_wait_bounded(&bar[bs], (gt >> 1) & 1);
+			if (__syncthreads_or(!ok)) {
+				timed_out = true;
+				break;
+			}
+			if (tid == 0 && t + 1 < nt) {
+				const int bn = (gt + 1) & 1;
+				const int64_t jt = jt0 + t + 1;
+				mbar_arrive_expect_tx(&bar[bn], NP * TILE_BYTES);
+				bulk_g2s(smem_tiles + (bn * NP) * J, jsrc + jt * J, TILE_BYTES, &bar[bn]);
+				if (NP == 2)
+					bulk_g2s(smem_tiles + (bn * NP + 1) * J, jsrclo + jt * J, TILE_BYTES, &bar[bn]);
+			}
+			const float4* __restrict__ sj = smem_tiles + (bs * NP) * J;
+			const float4* __restrict__ sl = sj + J;
+#pragma unroll 4
+			for (int j = 0; j < J; ++j) {
+				const float4 pj = sj[j];
+				float4 lj = make_float4(0.f, 0.f, 0.f, 0.f);
+				if (NP == 2) lj = sl[j];
+#pragma unroll
+				for (int k = 0; k < B; ++k) {
+					float dx = pj.x - xi[k];
+					float dy = pj.y - yi[k];
+					float dz = pj.z - zi[k];
+					if (NP == 2) {
+						dx = dx + (lj.x - xl[k]);
+						dy = dy + (lj.y - yl[k]);
+						dz = dz + (lj.z - zl[k]);
+					}
+					const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+					const float inv = rsqrt_sfu(r2);
+					const float inv2 = inv * inv;
+					float w = pj.w * inv;
+					w = w * inv2;
+					fx[k] = fmaf(dx, w, fx[k]);
+					fy[k] = fmaf(dy, w, fy[k]);
+					fz[k] = fmaf(dz, w, fz[k]);
+				}
+			}
+#pragma unroll
+			for (int k = 0; k < B; ++k) {
+				ax[k] += static_cast<double>(fx[k]);
+				ay[k] += static_cast<double>(fy[k]);
+				az[k] += static_cast<double>(fz[k]);
+				fx[k] = fy[k] = fz[k] = 0.f;
+			}
+		}
+		if (timed_out) break;
+
+		// FP64 partial of this CTA's piece of the segment
+		const int64_t slot = S.slot_base + (c - S.cta_first);
+		double* __restrict__ out = b.part + slot * 3 * IT;
+#pragma unroll
+		for (int k = 0; k < B; ++k) {
+			out[tid + k * T] = ax[k];
+			out[IT + tid + k * T] = ay[k];
+			out[2 * IT + tid + k * T] = az[k];
+		}
+		ub = S.unit_begin + jt1;
+		++s;
+	}
+
+	if (timed_out && tid == 0) {
+		set_error(b.err, GRAV_DEV_TIMEOUT);
+		// the copy that did not arrive is the only one in flight; give it one more
+		// bounded wait so that it does not land in shared memory after this CTA exits
+		mbar_wait_bounded(&bar[gt & 1], (gt >> 1) & 1);
+	}
+}
+
+#define GRAV_F32_ENTRY(MODE, B, T, J) \
+	{MODE, B, T, J, reinterpret_cast<const void*>(&stage1_f32_kernel<MODE, B, T, J>), \
+		2 * ((MODE == GRAV_MODE_FP32C) ? 2 : 1) * J * 16}
+
+static const Stage1Kernel k_table_f32[] = {
+	GRAV_F32_ENTRY(GRAV_MODE_FP32, 1, 128, 128),
+	GRAV_F32_ENTRY(GRAV_MODE_FP32, 2, 128, 128),
+	GRAV_F32_ENTRY(GRAV_MODE_FP32, 4, 128, 128),
+	GRAV_F32_ENTRY(GRAV_MODE_FP32, 4, 128, 256),
+	GRAV_F32_ENTRY(GRAV_MODE_FP32, 8, 128, 256),
+	GRAV_F32_ENTRY(GRAV_MODE_FP32, 2, 256, 256),
+	GRAV_F32_ENTRY(GRAV_MODE_FP32, 4, 256, 256),
+	GRAV_F32_ENTRY(GRAV_MODE_FP32, 8, 256, 256),
+	GRAV_F32_ENTRY(GRAV_MODE_FP32C, 1, 128, 128),
+	GRAV_F32_ENTRY(GRAV_MODE_FP32C, 2, 128, 128),
+	GRAV_F32_ENTRY(GRAV_MODE_FP32C, 4, 128, 256),
+	GRAV_F32_ENTRY(GRAV_MODE_FP32C, 4, 256, 256),
+};
+
+int stage1_table_f32(const Stage1Kernel** out)
+{
+	*out = k_table_f32;
+	return static_cast<int>(sizeof(k_table_f32) / sizeof(k_table_f32[0]));
+}
+
+}  // namespace grav

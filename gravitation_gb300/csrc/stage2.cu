@@ -1,0 +1,96 @@
+// stage2.cu -- stage 2 of the step and the refresh of the stage-1 positions.
+//
+// One thread per row of the padded position array.  For a real body it adds the
+// FP64 partial-sum slots of its segment in slot order (deterministic), then applies
+// the base class's update in FP64 with separately rounded products and sums,
+//     v = a*T + v ;  r = v*T + r          (_base_.py:58-62, np2.py:110-115)
+// exactly as the reference's Python floats / numpy arrays round them, and finally
+// rewrites the row of the stage-1 position array (FP32 hi[, lo] or FP64).  Padding
+// rows get zeros (G*m = 0), so padded j-tiles contribute nothing.
+#include "grav_device.cuh"
+
+namespace grav {
+
+struct __align__(32) drow4 {
+	double x, y, z, w;
+};
+
+__global__ void __launch_bounds__(256) stage2_kernel(const grav_batch b, const int flags)
+{
+	const int64_t g = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (g >= b.n_pad_total) return;
+	const int IT = b.tile.bpt * b.tile.threads;
+	const int64_t seg = g / IT;
+	const int li = static_cast<int>(g - seg * IT);
+	const grav_seg_desc S = b.seg[seg];
+	const grav_univ_desc U = b.univ[S.u];
+	const int il = S.il0 + li;
+
+	if (il >= U.n) {
+		if (b.mode == GRAV_MODE_FP64) {
+			static_cast<drow4*>(b.pos)[g] = drow4{0.0, 0.0, 0.0, 0.0};
+		} else {
+			float4* p = static_cast<float4*>(b.pos);
+			p[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+			if (b.mode == GRAV_MODE_FP32C) p[b.n_pad_total + g] = make_float4(0.f, 0.f, 0.f, 0.f);
+		}
+		return;
+	}
+
+	const int64_t row = U.body_off + il;
+	drow4* rr = reinterpret_cast<drow4*>(b.r);
+	drow4 r = rr[row];
+
+	if (!(flags & GRAV_S2_PREPARE)) {
+		double ax = 0.0, ay = 0.0, az = 0.0;
+		const double* __restrict__ part = b.part;
+		for (int k = 0; k < S.nslots; ++k) {
+			const int64_t base = static_cast<int64_t>(S.slot_base + k) * 3 * IT + li;
+			ax += part[base];
+			ay += part[base + IT];
+			az += part[base + 2 * IT];
+		}
+		if ((flags & GRAV_S2_WRITE_A) && b.a_out)
+			reinterpret_cast<drow4*>(b.a_out)[row] = drow4{ax, ay, az, 0.0};
+		if (flags & GRAV_S2_INTEGRATE) {
+			drow4* vv = reinterpret_cast<drow4*>(b.v);
+			drow4 v = vv[row];
+			const double T = U.T;
+			v.x = __dadd_rn(__dmul_rn(ax, T), v.x);
+			v.y = __dadd_rn(__dmul_rn(ay, T), v.y);
+			v.z = __dadd_rn(__dmul_rn(az, T), v.z);
+			r.x = __dadd_rn(__dmul_rn(v.x, T), r.x);
+			r.y = __dadd_rn(__dmul_rn(v.y, T), r.y);
+			r.z = __dadd_rn(__dmul_rn(v.z, T), r.z);
+			vv[row] = v;
+			rr[row] = r;
+		}
+	}
+
+	if (b.mode == GRAV_MODE_FP64) {
+		static_cast<drow4*>(b.pos)[g] = r;
+	} else {
+		float4* p = static_cast<float4*>(b.pos);
+		const float hx = __double2float_rn(r.x);
+		const float hy = __double2float_rn(r.y);
+		const float hz = __double2float_rn(r.z);
+		p[g] = make_float4(hx, hy, hz, __double2float_rn(r.w));
+		if (b.mode == GRAV_MODE_FP32C) {
+			p[b.n_pad_total + g] = make_float4(
+				__double2float_rn(__dsub_rn(r.x, static_cast<double>(hx))),
+				__double2float_rn(__dsub_rn(r.y, static_cast<double>(hy))),
+				__double2float_rn(__dsub_rn(r.z, static_cast<double>(hz))), 0.f);
+		}
+	}
+}
+
+cudaError_t launch_stage2(const grav_batch& b, int flags, cudaStream_t stream)
+{
+	if (b.n_pad_total == 0) return cudaSuccess;
+	const int threads = 256;
+	const int64_t blocks = (b.n_pad_total + threads - 1) / threads;
+	stage2_kernel<<<static_cast<unsigned>(blocks), threads, 0, stream>>>(b, flags);
+	return cudaGetLastError();
+}
+
+}  // namespace grav

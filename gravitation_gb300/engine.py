@@ -1,0 +1,272 @@
+"""Device engine: FP64 state, work-list plan and stage launches for one or more universes.
+
+PyTorch owns every device buffer; the C ABI (libgravgb300.so) borrows raw pointers.
+One ``Engine`` holds a packed batch of universes (a single universe is a batch of
+one) and drives the persistent stage-1 kernel and the FP64 stage-2 kernel on a CUDA
+stream.  There is no CPU path: without the library or a GB300 every call raises.
+
+Layout in HBM (all packed universe after universe):
+  r, v     float64 [n_bodies, 4]   (x, y, z, G*m) and (vx, vy, vz, 0)
+  pos      padded stage-1 positions: float4 hi (+ float4 lo in fp32c) or double4
+  part     float64 [n_slots, 3, itile]  FP64 partial sums written by stage 1
+  univ/seg plan tables (grav_univ_desc / grav_seg_desc)
+"""
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import check
+
+_DEVICE_CACHE = {}
+
+
+class DeviceInfo:
+    def __init__(self, index, sm_count, cc):
+        self.index = index
+        self.sm_count = sm_count
+        self.cc = cc
+        self.name = torch.cuda.get_device_name(index)
+
+    def __repr__(self):
+        return 'DeviceInfo(%d, %s, sms=%d, cc=%d.%d)' % (
+            self.index, self.name, self.sm_count, self.cc[0], self.cc[1])
+
+
+def device_info(device=None):
+    """SM count and compute capability; raises unless the GPU is sm_103 (GB300)."""
+    if not torch.cuda.is_available():
+        raise RuntimeError('gravitation_gb300 needs a CUDA GPU (GB300); none is visible')
+    index = torch.device('cuda', torch.cuda.current_device()).index if device is None else \
+        torch.device(device).index
+    if index is None:
+        index = torch.cuda.current_device()
+    if index not in _DEVICE_CACHE:
+        L = _lib.load()
+        sms, ma, mi = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        with torch.cuda.device(index):
+            check(L.grav_device_query(index, ctypes.byref(sms), ctypes.byref(ma), ctypes.byref(mi)))
+        _DEVICE_CACHE[index] = DeviceInfo(index, sms.value, (ma.value, mi.value))
+    return _DEVICE_CACHE[index]
+
+
+def tile_list(mode):
+    L = _lib.load()
+    m = _lib.MODES[mode] if isinstance(mode, str) else mode
+    n = L.grav_tile_list(m, None, 0)
+    if n < 0:
+        check(n)
+    arr = (_lib.Tile * n)()
+    L.grav_tile_list(m, arr, n)
+    return [_lib.Tile(t.bpt, t.threads, t.jtile, 0) for t in arr]
+
+
+def occupancy(mode, tile, device=None):
+    L = _lib.load()
+    m = _lib.MODES[mode] if isinstance(mode, str) else mode
+    out = ctypes.c_int32()
+    info = device_info(device)
+    with torch.cuda.device(info.index):
+        check(L.grav_occupancy(m, ctypes.byref(tile), ctypes.byref(out)))
+    return out.value
+
+
+def make_plan(sizes, T, tile):
+    """Host-side plan (no GPU needed): (PlanInfo, univ ctypes array, seg ctypes array)."""
+    L = _lib.load()
+    sizes = [int(x) for x in sizes]
+    nu = len(sizes)
+    n_arr = (ctypes.c_int32 * max(nu, 1))(*sizes)
+    T_list = list(T) if np.ndim(T) else [float(T)] * nu
+    T_arr = (ctypes.c_double * max(nu, 1))(*[float(x) for x in T_list])
+    info = _lib.PlanInfo()
+    check(L.grav_plan(nu, n_arr, T_arr, ctypes.byref(tile), ctypes.byref(info), None, None))
+    univ = (_lib.UnivDesc * max(info.n_univ, 1))()
+    seg = (_lib.SegDesc * max(info.n_seg, 1))()
+    check(L.grav_plan(nu, n_arr, T_arr, ctypes.byref(tile), ctypes.byref(info), univ, seg))
+    return info, univ, seg
+
+
+def _ctypes_to_device(arr, nbytes, device):
+    host = torch.frombuffer(bytearray(ctypes.string_at(ctypes.addressof(arr), nbytes)),
+                            dtype=torch.uint8) if nbytes else torch.zeros(0, dtype=torch.uint8)
+    dev = torch.empty(max(nbytes, 16), dtype=torch.uint8, device=device)
+    if nbytes:
+        dev[:nbytes].copy_(host)
+    return dev
+
+
+def default_tile(mode, sizes, device=None):
+    """Tile shape used when no tuned entry exists: the largest i-tile that still gives
+    every resident CTA several work units."""
+    info = device_info(device)
+    cands = tile_list(mode)
+    best = None
+    for t in cands:
+        occ = occupancy(mode, t, device)
+        if occ <= 0:
+            continue
+        grid = info.sm_count * occ
+        t.grid = grid
+        pinfo, _, _ = make_plan(sizes, 1.0, t)
+        if pinfo.n_units == 0:
+            continue
+        # padded work (interactions) and the slowest CTA's share of it
+        work = pinfo.n_units * pinfo.itile * t.jtile
+        per_cta = -(-pinfo.n_units // min(grid, pinfo.n_units)) * pinfo.itile * t.jtile
+        # register-blocked shapes issue fewer shared loads per interaction
+        eff = {1: 0.80, 2: 0.90, 4: 0.97, 8: 1.0}.get(t.bpt, 0.9)
+        score = per_cta / eff + 0.02 * work / grid
+        if best is None or score < best[0]:
+            best = (score, _lib.Tile(t.bpt, t.threads, t.jtile, grid))
+    if best is None:
+        raise RuntimeError('no compiled tile shape fits mode %r' % (mode,))
+    return best[1]
+
+
+class Engine:
+    """Packed batch of universes on one GB300 with FP64 state.
+
+    Parameters
+      sizes : list of body counts (one per universe)
+      T     : time step (scalar or one per universe)
+      mode  : 'fp32' (default), 'fp32c' or 'fp64'
+      tile  : _lib.Tile, or None to use the autotuner's choice / the default shape
+    """
+
+    def __init__(self, sizes, T, mode='fp32', tile=None, device=None, tuner=None):
+        self.lib = _lib.load()
+        self.dev_info = device_info(device)
+        self.device = torch.device('cuda', self.dev_info.index)
+        if isinstance(mode, str):
+            if mode not in _lib.MODES:
+                raise ValueError('unknown precision mode %r (fp32, fp32c, fp64)' % mode)
+            self.mode_name, self.mode = mode, _lib.MODES[mode]
+        else:
+            self.mode = int(mode)
+            self.mode_name = {v: k for k, v in _lib.MODES.items()}[self.mode]
+        self.sizes = [int(x) for x in sizes]
+        self.T = list(T) if np.ndim(T) else [float(T)] * len(self.sizes)
+        if tile is None:
+            if tuner is not None:
+                tile = tuner.choose(self.mode_name, self.sizes, self.dev_info)
+            else:
+                tile = default_tile(self.mode_name, self.sizes, self.dev_info.index)
+        elif tile.grid <= 0:
+            tile = _lib.Tile(tile.bpt, tile.threads, tile.jtile,
+                             self.dev_info.sm_count * occupancy(self.mode, tile, self.dev_info.index))
+        if not self.lib.grav_tile_supported(self.mode, ctypes.byref(tile)):
+            raise ValueError('tile %r is not compiled for mode %s' % (tile, self.mode_name))
+        self.tile = tile
+        self.info, univ, seg = make_plan(self.sizes, self.T, tile)
+        info = self.info
+        dev = self.device
+        self.univ_dev = _ctypes_to_device(univ, ctypes.sizeof(_lib.UnivDesc) * info.n_univ, dev)
+        self.seg_dev = _ctypes_to_device(seg, ctypes.sizeof(_lib.SegDesc) * info.n_seg, dev)
+        self.univ_host = univ
+        self.seg_host = seg
+        nb = max(info.n_bodies, 1)
+        self.r = torch.zeros((nb, 4), dtype=torch.float64, device=dev)
+        self.v = torch.zeros((nb, 4), dtype=torch.float64, device=dev)
+        self.a = torch.zeros((nb, 4), dtype=torch.float64, device=dev)
+        pos_bytes = int(self.lib.grav_pos_bytes(self.mode, info.n_pad_total))
+        self.pos = torch.zeros(max(pos_bytes // 4, 4), dtype=torch.float32, device=dev)
+        part_bytes = int(self.lib.grav_part_bytes(ctypes.byref(info)))
+        self.part = torch.zeros(max(part_bytes // 8, 1), dtype=torch.float64, device=dev)
+        self.err = torch.zeros(1, dtype=torch.int32, device=dev)
+        b = _lib.Batch()
+        b.mode = self.mode
+        b.n_univ = info.n_univ
+        b.n_seg = info.n_seg
+        b.n_slots = info.n_slots
+        b.n_bodies = info.n_bodies
+        b.n_pad_total = info.n_pad_total
+        b.n_units = info.n_units
+        b.tile = _lib.Tile(tile.bpt, tile.threads, tile.jtile, info.grid)
+        b.eps2 = 1e-30
+        b.univ = self.univ_dev.data_ptr()
+        b.seg = self.seg_dev.data_ptr()
+        b.r = self.r.data_ptr()
+        b.v = self.v.data_ptr()
+        b.pos = self.pos.data_ptr()
+        b.part = self.part.data_ptr()
+        b.a_out = self.a.data_ptr()
+        b.err = self.err.data_ptr()
+        self.batch = b
+        self._bref = ctypes.byref(b)
+        self.offsets = np.array([u.body_off for u in list(univ)[:info.n_univ]], dtype=np.int64)
+
+    # ---- state ----------------------------------------------------------------------
+    def set_state(self, r, v, gm, stream=None):
+        """Load positions, velocities and G*m (already scaled) for all bodies, packed."""
+        n = self.info.n_bodies
+        r = torch.as_tensor(np.asarray(r, dtype=np.float64).reshape(n, 3) if not torch.is_tensor(r)
+                            else r.reshape(n, 3), dtype=torch.float64)
+        v = torch.as_tensor(np.asarray(v, dtype=np.float64).reshape(n, 3) if not torch.is_tensor(v)
+                            else v.reshape(n, 3), dtype=torch.float64)
+        gm = torch.as_tensor(np.asarray(gm, dtype=np.float64).reshape(n) if not torch.is_tensor(gm)
+                             else gm.reshape(n), dtype=torch.float64)
+        if not bool(torch.isfinite(gm).all()) or bool((gm < 0).any()):
+            raise ValueError('G*m must be finite and >= 0')
+        max_gm = float(gm.max()) if n else 0.0
+        self.batch.eps2 = float(self.lib.grav_eps2(max_gm))
+        with torch.cuda.stream(self._stream(stream)):
+            self.r[:n, :3].copy_(r, non_blocking=False)
+            self.r[:n, 3].copy_(gm)
+            self.v[:n, :3].copy_(v)
+            self.v[:n, 3].zero_()
+        self.prepare(stream)
+
+    def _stream(self, stream):
+        return stream if stream is not None else torch.cuda.current_stream(self.device)
+
+    def _h(self, stream):
+        return ctypes.c_void_p(self._stream(stream).cuda_stream)
+
+    # ---- stages ---------------------------------------------------------------------
+    def prepare(self, stream=None):
+        """Refresh the padded stage-1 positions after r was changed."""
+        check(self.lib.grav_prepare(self._bref, self._h(stream)))
+
+    def stage1(self, stream=None):
+        check(self.lib.grav_stage1(self._bref, self._h(stream)))
+
+    def stage2(self, flags=_lib.GRAV_S2_INTEGRATE, stream=None):
+        check(self.lib.grav_stage2(self._bref, int(flags), self._h(stream)))
+
+    def step(self, steps=1, stream=None, write_a=False):
+        """`steps` full steps (stage 1 + stage 2) queued on the stream."""
+        flags = _lib.GRAV_S2_INTEGRATE | (_lib.GRAV_S2_WRITE_A if write_a else 0)
+        h = self._h(stream)
+        for _ in range(int(steps)):
+            check(self.lib.grav_step(self._bref, flags, h))
+
+    def forces(self, stream=None):
+        """Stage 1 only; returns the accelerations (float64 [n_bodies, 3], device)."""
+        self.stage1(stream)
+        self.stage2(_lib.GRAV_S2_WRITE_A, stream)
+        return self.a[:self.info.n_bodies, :3]
+
+    # ---- errors ---------------------------------------------------------------------
+    def device_error(self):
+        """Device error flag (GRAV_DEV_*); synchronises the stream."""
+        return int(self.err.item())
+
+    def raise_on_device_error(self):
+        code = self.device_error()
+        if code != _lib.GRAV_DEV_OK:
+            self.err.zero_()
+            raise _lib.GravError(_lib.GRAV_E_CUDA, 'device error flag %d (%s)' % (
+                code, 'bounded wait for a bulk copy expired' if code == _lib.GRAV_DEV_TIMEOUT
+                else 'unknown'))
+
+    # ---- views ----------------------------------------------------------------------
+    def universe_slice(self, u):
+        o = int(self.offsets[u])
+        return slice(o, o + self.sizes[u])
+
+    def interactions_per_step(self):
+        """Algorithmic interactions per step: sum over universes of N^2."""
+        return sum(n * n for n in self.sizes)

@@ -1,0 +1,137 @@
+"""GB300 implementation of the plugin hooks of ``universe_base``.
+
+``GB300Stages`` is mixed in front of ``universe_base`` by the ``gb1`` kernel package
+(class universe(GB300Stages, universe_base)).  It overrides only the hooks the
+reference lets kernels override (_base_.py:131-177): start_kernel, step_stage1,
+step_stage2 and stop_kernel.  ``__init__``, ``add_object``, ``step`` and iteration
+stay the base class's.
+
+Behaviour seen from the front end (README.md:50, worker.py:119-136):
+  - after every step() the position and velocity of each point mass are valid
+    iterables: ``pm._r`` / ``pm._v`` are numpy row views of a pinned FP64 host mirror
+    (the binding pattern of np2.py:70-75);
+  - step() is synchronous, so wall-clock timing of step() is valid;
+  - with host_sync='full' (default) the mirror is the source of truth: edits of
+    pm._r / pm._v between steps are uploaded at the next step, as the reference's
+    kernels re-read pm._r every stage 1 (np1.py:101-102, pc2.py:147-151).
+
+Kernel options (keyword arguments of the constructor, kept in self._meta):
+  precision  'fp32' | 'fp32c' | 'fp64'   default from dtype ('float32'->fp32,
+             'float64'->fp64)
+  host_sync  'full' (upload + download every step) | 'pull' (download only) |
+             'none' (device state only; call sync_host() to refresh the mirror)
+  fuse       True (default): stage 1 and stage 2 both run in step_stage1 on the GPU
+             and step_stage2 refreshes the mirror; False: step_stage1 fills pm._a
+             like the reference's kernels and step_stage2 integrates on the GPU
+  tile       (bpt, threads, jtile) to force a tile shape; default: autotuned
+  autotune   True (default) to use the autotuner cache / tuning
+  device     CUDA device index (default: current device)
+"""
+
+import numpy as np
+import torch
+
+from . import _lib
+from .engine import Engine
+
+_DTYPE_MODE = {'float32': 'fp32', 'float64': 'fp64'}
+
+
+class GB300Stages:
+    """start/step/stop hooks of a gravitation kernel running on one GB300."""
+
+    def start_kernel(self):
+        meta = self._meta
+        mode = meta.get('precision') or _DTYPE_MODE.get(str(self._dtype))
+        if mode not in _lib.MODES:
+            raise ValueError('unsupported dtype/precision %r (float32, float64, fp32, fp32c, '
+                             'fp64)' % (meta.get('precision') or self._dtype,))
+        self._gb_sync = meta.get('host_sync', 'full')
+        if self._gb_sync not in ('full', 'pull', 'none'):
+            raise ValueError('host_sync must be full, pull or none')
+        self._gb_fuse = bool(meta.get('fuse', True))
+        n = len(self._mass_list)
+        if n == 0:
+            raise ValueError('no point masses were added before start()')
+        tile = meta.get('tile')
+        tuner = None
+        if tile is not None:
+            tile = _lib.Tile(int(tile[0]), int(tile[1]), int(tile[2]), 0)
+        elif meta.get('autotune', True):
+            from .tune import default_tuner
+            tuner = default_tuner()
+        device = meta.get('device')
+        self._gb = Engine([n], float(self._T), mode=mode, tile=tile, device=device, tuner=tuner)
+        dev = self._gb.device
+        # pinned FP64 host mirror (x, y, z, G*m) / (vx, vy, vz, 0) / (ax, ay, az, 0)
+        pin = torch.cuda.is_available()
+        self._gb_hr = torch.zeros((n, 4), dtype=torch.float64, pin_memory=pin)
+        self._gb_hv = torch.zeros((n, 4), dtype=torch.float64, pin_memory=pin)
+        self._gb_ha = torch.zeros((n, 4), dtype=torch.float64, pin_memory=pin)
+        hr, hv, ha = self._gb_hr.numpy(), self._gb_hv.numpy(), self._gb_ha.numpy()
+        for i, pm in enumerate(self._mass_list):
+            hr[i, :3] = pm._r[:3]
+            hr[i, 3] = self._G * pm._m
+            hv[i, :3] = pm._v[:3]
+        if not np.all(np.isfinite(hr)) or not np.all(np.isfinite(hv)):
+            raise ValueError('positions, velocities and masses must be finite')
+        self._gb_stream = torch.cuda.Stream(device=dev)
+        self._gb.set_state(hr[:, :3], hv[:, :3], hr[:, 3], stream=self._gb_stream)
+        self._gb_stream.synchronize()
+        # np2-style binding: the point masses see rows of the host mirror
+        for i, pm in enumerate(self._mass_list):
+            pm._r = hr[i, :3]
+            pm._v = hv[i, :3]
+            pm._a = ha[i, :3]
+
+    # ---- stages ----------------------------------------------------------------------
+    def _gb_upload(self):
+        g, s = self._gb, self._gb_stream
+        with torch.cuda.stream(s):
+            g.r.copy_(self._gb_hr, non_blocking=True)
+            g.v.copy_(self._gb_hv, non_blocking=True)
+        g.prepare(stream=s)
+
+    def _gb_download(self, with_a=False):
+        g, s = self._gb, self._gb_stream
+        with torch.cuda.stream(s):
+            self._gb_hr.copy_(g.r, non_blocking=True)
+            self._gb_hv.copy_(g.v, non_blocking=True)
+            if with_a:
+                self._gb_ha.copy_(g.a, non_blocking=True)
+        s.synchronize()
+        self._gb.raise_on_device_error()
+
+    def step_stage1(self):
+        if self._gb_sync == 'full':
+            self._gb_upload()
+        if self._gb_fuse:
+            self._gb.step(1, stream=self._gb_stream)
+        else:
+            g, s = self._gb, self._gb_stream
+            g.stage1(stream=s)
+            g.stage2(_lib.GRAV_S2_WRITE_A, stream=s)
+            with torch.cuda.stream(s):
+                self._gb_ha.copy_(g.a, non_blocking=True)
+            s.synchronize()
+            g.raise_on_device_error()
+
+    def step_stage2(self):
+        if not self._gb_fuse:
+            self._gb.stage2(_lib.GRAV_S2_INTEGRATE, stream=self._gb_stream)
+        if self._gb_sync in ('full', 'pull'):
+            self._gb_download()
+        else:
+            self._gb_stream.synchronize()
+        # the base class's stage 2 leaves the accelerations zeroed (_base_.py:62)
+        self._gb_ha[:, :3] = 0.0
+
+    def sync_host(self):
+        """Refresh the host mirror (pm._r, pm._v) from the device state."""
+        self._gb_download()
+
+    def stop_kernel(self):
+        if getattr(self, '_gb', None) is not None:
+            self._gb_stream.synchronize()
+            self._gb_download()
+            self._gb = None

@@ -1,0 +1,170 @@
+"""Autotuner for the stage-1 tile shape (bodies per thread, threads per CTA, j-tile).
+
+For a workload key -- the GPU (name, SM count), the precision mode, the library's
+source hash and the size bucket (single universe: N rounded up to a power of two;
+batch: a signature of the size list) -- every compiled tile shape is timed with CUDA
+events on a seeded synthetic state of that size and the fastest is cached as JSON.
+
+Cache robustness: an unreadable or malformed cache file is ignored (and rewritten),
+entries from another library build (different source hash) or naming a tile that is
+not compiled are ignored, and nothing is trusted that does not pass
+``grav_tile_supported``.  The cache path is $GRAV_TUNE_CACHE or
+gravitation_gb300/_tune_cache.json.
+"""
+
+import hashlib
+import json
+import os
+import tempfile
+import threading
+
+import numpy as np
+
+from . import _lib
+from .build import source_hash
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def bucket_of(sizes):
+    sizes = [int(s) for s in sizes]
+    if len(sizes) == 1:
+        n = max(sizes[0], 1)
+        return 'single:%d' % (1 << (n - 1).bit_length())
+    h = hashlib.sha1(np.asarray(sorted(sizes), dtype=np.int64).tobytes()).hexdigest()[:12]
+    return 'batch:%d:%s' % (len(sizes), h)
+
+
+class Tuner:
+    def __init__(self, path=None, build_hash=None):
+        self.path = path or os.environ.get('GRAV_TUNE_CACHE') or os.path.join(
+            HERE, '_tune_cache.json')
+        self._build_hash = build_hash
+        self._lock = threading.Lock()
+        self._cache = None
+
+    @property
+    def build_hash(self):
+        if self._build_hash is None:
+            self._build_hash = source_hash()
+        return self._build_hash
+
+    # ---- cache ----------------------------------------------------------------------
+    def load(self):
+        if self._cache is not None:
+            return self._cache
+        data = {}
+        try:
+            with open(self.path) as f:
+                raw = json.load(f)
+            if isinstance(raw, dict) and isinstance(raw.get('entries'), dict):
+                data = raw['entries']
+        except (OSError, ValueError):
+            data = {}
+        self._cache = data
+        return data
+
+    def save(self):
+        data = {'format': 1, 'entries': self._cache or {}}
+        d = os.path.dirname(os.path.abspath(self.path))
+        os.makedirs(d, exist_ok=True)
+        fd, tmp = tempfile.mkstemp(dir=d, prefix='.tune', suffix='.json')
+        with os.fdopen(fd, 'w') as f:
+            json.dump(data, f, indent=1, sort_keys=True)
+        os.replace(tmp, self.path)
+
+    def key(self, mode, sizes, dev_info):
+        return '|'.join([dev_info.name, str(dev_info.sm_count), mode, bucket_of(sizes),
+                         self.build_hash])
+
+    def lookup(self, mode, sizes, dev_info):
+        """Cached tile for the key, or None (missing, stale or invalid entry)."""
+        ent = self.load().get(self.key(mode, sizes, dev_info))
+        if not isinstance(ent, dict):
+            return None
+        try:
+            t = _lib.Tile(int(ent['bpt']), int(ent['threads']), int(ent['jtile']), int(ent['grid']))
+        except (KeyError, TypeError, ValueError):
+            return None
+        if t.grid <= 0:
+            return None
+        L = _lib.load()
+        m = _lib.MODES[mode]
+        import ctypes
+        if not L.grav_tile_supported(m, ctypes.byref(t)):
+            return None
+        return t
+
+    def store(self, mode, sizes, dev_info, tile, ms):
+        with self._lock:
+            self.load()[self.key(mode, sizes, dev_info)] = {
+                'bpt': tile.bpt, 'threads': tile.threads, 'jtile': tile.jtile,
+                'grid': tile.grid, 'ms': ms}
+            self.save()
+
+    # ---- tuning ---------------------------------------------------------------------
+    def choose(self, mode, sizes, dev_info, tune_if_missing=None):
+        """Tile for the workload: cached, else tuned (if enabled), else the default."""
+        from .engine import default_tile
+        t = self.lookup(mode, sizes, dev_info)
+        if t is not None:
+            return t
+        if tune_if_missing is None:
+            tune_if_missing = os.environ.get('GRAV_AUTOTUNE', '1') != '0'
+        if tune_if_missing:
+            return self.tune(mode, sizes, dev_info)
+        return default_tile(mode, sizes, dev_info.index)
+
+    def tune(self, mode, sizes, dev_info, reps=5, grid_factors=(1,)):
+        """Time every compiled tile shape on a seeded state and cache the fastest."""
+        import torch
+        from .engine import Engine, occupancy, tile_list
+        from .scenarios import uniform_cube
+        sizes = [int(s) for s in sizes]
+        rs, vs, ms = [], [], []
+        for u, n in enumerate(sizes):
+            r, v, m = uniform_cube(n, seed=1000 + u)
+            rs.append(r)
+            vs.append(v)
+            ms.append(m * 6.6740831e-11)
+        r = np.concatenate(rs) if rs else np.zeros((0, 3))
+        v = np.concatenate(vs) if vs else np.zeros((0, 3))
+        gm = np.concatenate(ms) if ms else np.zeros(0)
+        best = None
+        for cand in tile_list(mode):
+            occ = occupancy(mode, cand, dev_info.index)
+            if occ <= 0:
+                continue
+            for gf in grid_factors:
+                t = _lib.Tile(cand.bpt, cand.threads, cand.jtile, dev_info.sm_count * occ * gf)
+                eng = Engine(sizes, 1.0, mode=mode, tile=t, device=dev_info.index)
+                eng.set_state(r, v, gm)
+                s = torch.cuda.current_stream(eng.device)
+                eng.stage1()
+                eng.stage1()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(s)
+                for _ in range(reps):
+                    eng.stage1()
+                e1.record(s)
+                e1.synchronize()
+                eng.raise_on_device_error()
+                ms_ = e0.elapsed_time(e1) / reps
+                if best is None or ms_ < best[0]:
+                    best = (ms_, _lib.Tile(t.bpt, t.threads, t.jtile, t.grid))
+                del eng
+        if best is None:
+            raise RuntimeError('no tile shape could be timed for mode %s' % mode)
+        self.store(mode, sizes, dev_info, best[1], best[0])
+        return best[1]
+
+
+_DEFAULT = None
+
+
+def default_tuner():
+    global _DEFAULT
+    if _DEFAULT is None:
+        _DEFAULT = Tuner()
+    return _DEFAULT

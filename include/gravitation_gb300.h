@@ -1,0 +1,205 @@
+/*
+ * gravitation_gb300.h -- C ABI of the GB300 all-pairs n-body engine (libgravgb300.so).
+ *
+ * The library is the stage-1/stage-2 hot path of one time step of the reference's
+ * plugin API (gravitation/kernel/_base_.py:136-156): stage 1 computes
+ *     a_i = sum_{j != i} G m_j (r_j - r_i) / |r_j - r_i|^3
+ * and stage 2 applies the base class's symplectic Euler update
+ *     v = a*T + v ;  r = v*T + r          (_base_.py:58-62)
+ * on device memory owned by the caller.  Plain pointers and sizes only.
+ *
+ * Conventions
+ *   - Every entry point returns 0 on success and a negative GRAV_E_* code on failure;
+ *     grav_last_error() then describes the failure (thread-local string).
+ *   - The library allocates no memory.  The caller owns every buffer; device buffers
+ *     must stay valid until the work queued on `stream` has completed.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *   - Bodies are stored packed, universe after universe, as rows of 4 doubles:
+ *       r[i] = (x, y, z, G*m)   and   v[i] = (vx, vy, vz, 0)
+ *     with G already scaled as in _base_.py:85-88 and r, v, m scaled as in
+ *     _base_.py:114-117.  The engine works on this FP64 state; stage 1 reads a padded
+ *     copy of the positions (FP32 or FP64 by precision mode) that stage 2 refreshes.
+ *   - Bodies at zero separation (the self pair and coincident distinct bodies) exert
+ *     no force on each other.  The reference divides by zero there (np1.py:85-88).
+ */
+#ifndef GRAVITATION_GB300_H
+#define GRAVITATION_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GRAV_ABI_VERSION 1
+
+/* status codes */
+#define GRAV_OK 0
+#define GRAV_E_ARG -1         /* invalid argument (null pointer, bad size, bad mode) */
+#define GRAV_E_TILE -2        /* tile shape not compiled into this library */
+#define GRAV_E_CUDA -3        /* a CUDA runtime call failed */
+#define GRAV_E_SIZE -4        /* caller buffer too small */
+#define GRAV_E_DEVICE -5      /* device is not a GB300-class (sm_103) GPU */
+
+/* device error flag values written by kernels into grav_batch.err */
+#define GRAV_DEV_OK 0
+#define GRAV_DEV_TIMEOUT 1    /* a bounded wait for a bulk copy expired */
+
+/* precision modes (universe_base dtype / kernel meta "precision") */
+#define GRAV_MODE_FP32 0      /* FP32 separations and weights, FP32 tile partials summed in FP64 */
+#define GRAV_MODE_FP32C 1     /* as FP32 with double-single (hi+lo) positions: separations exact */
+#define GRAV_MODE_FP64 2      /* FP64 throughout */
+
+/* stage-2 flags */
+#define GRAV_S2_INTEGRATE 1   /* v = a*T + v ; r = v*T + r */
+#define GRAV_S2_WRITE_A 2     /* write the accelerations to a_out */
+#define GRAV_S2_PREPARE 4     /* only refresh the padded stage-1 positions from r */
+
+/* One universe of a packed batch (device array, built by grav_plan). */
+typedef struct grav_univ_desc {
+	int64_t body_off;  /* first row of this universe in r, v, a_out */
+	int64_t pad_off;   /* first row in the padded stage-1 position array */
+	int32_t n;         /* number of bodies */
+	int32_t n_jtiles;  /* ceil(n / jtile) */
+	double T;          /* time step of this universe */
+} grav_univ_desc;
+
+/* One i-tile of one universe: the unit of the persistent work list (device array). */
+typedef struct grav_seg_desc {
+	int64_t unit_begin; /* index of its first work unit (one j-tile) in the global order */
+	int32_t u;          /* universe */
+	int32_t il0;        /* first local body of the i-tile */
+	int32_t n_units;    /* j-tiles to visit (0 for a tile made only of padding) */
+	int32_t cta_first;  /* first CTA of the persistent grid that works on it */
+	int32_t slot_base;  /* first FP64 partial-sum slot of this segment */
+	int32_t nslots;     /* number of CTAs that work on it (= slots) */
+} grav_seg_desc;
+
+/* Tile shape of the stage-1 kernel. */
+typedef struct grav_tile {
+	int32_t bpt;      /* i-bodies held in registers per thread */
+	int32_t threads;  /* threads per CTA */
+	int32_t jtile;    /* j-bodies per shared-memory tile (one bulk copy) */
+	int32_t grid;     /* persistent CTAs (clamped to the number of work units) */
+} grav_tile;
+
+/* Sizes derived by grav_plan. */
+typedef struct grav_plan_info {
+	int64_t n_bodies;    /* sum of n over universes (rows of r, v, a_out) */
+	int64_t n_pad_total; /* rows of the padded stage-1 position array */
+	int64_t n_units;     /* total work units (i-tile x j-tile) */
+	int32_t n_univ;
+	int32_t n_seg;       /* = n_pad_total / itile */
+	int32_t n_slots;     /* FP64 partial-sum slots (each 3 x itile doubles) */
+	int32_t itile;       /* bpt * threads */
+	int32_t pad_unit;    /* max(itile, jtile) */
+	int32_t grid;        /* CTAs actually launched */
+} grav_plan_info;
+
+/* Everything one stage-1/stage-2 launch needs.  All pointers are device pointers. */
+typedef struct grav_batch {
+	int32_t mode;                 /* GRAV_MODE_* */
+	int32_t n_univ;
+	int32_t n_seg;
+	int32_t n_slots;
+	int64_t n_bodies;
+	int64_t n_pad_total;
+	int64_t n_units;
+	grav_tile tile;               /* tile.grid = CTAs launched (grav_plan_info.grid) */
+	float eps2;                   /* r^2 floor for the FP32 modes (see grav_eps2) */
+	float _pad0;
+	const grav_univ_desc* univ;   /* n_univ */
+	const grav_seg_desc* seg;     /* n_seg */
+	double* r;                    /* n_bodies x 4 */
+	double* v;                    /* n_bodies x 4 */
+	void* pos;                    /* padded stage-1 positions, grav_pos_bytes() */
+	double* part;                 /* n_slots x 3 x itile */
+	double* a_out;                /* n_bodies x 4, may be NULL unless GRAV_S2_WRITE_A */
+	int32_t* err;                 /* one device int, GRAV_DEV_* (first error wins) */
+} grav_batch;
+
+/* ---- library ---------------------------------------------------------------- */
+
+/* ABI version (GRAV_ABI_VERSION).  No reference counterpart. */
+int grav_abi_version(void);
+
+/* Message describing the last failure on this thread (never NULL). */
+const char* grav_last_error(void);
+
+/* SM count and compute capability of `device`.  Fails with GRAV_E_DEVICE on a GPU
+ * other than compute capability 10.3 (the library holds sm_103a code only). */
+int grav_device_query(int device, int32_t* sm_count, int32_t* cc_major, int32_t* cc_minor);
+
+/* 1 if the tile shape is compiled for `mode`, else 0. */
+int grav_tile_supported(int mode, const grav_tile* tile);
+
+/* Number of compiled tile shapes for `mode`; fills up to `cap` entries of `out`. */
+int grav_tile_list(int mode, grav_tile* out, int cap);
+
+/* Resident CTAs per SM of the stage-1 kernel for `mode` and `tile` on the current
+ * device (the persistent grid is sm_count * this). */
+int grav_occupancy(int mode, const grav_tile* tile, int32_t* ctas_per_sm);
+
+/* ---- planning (host only, no GPU needed) ------------------------------------- */
+
+/*
+ * Lay out `n_univ` universes of sizes n[u] (time steps T[u]) for the persistent
+ * stage-1 kernel with the given tile.  Two-call protocol: call with univ_out and
+ * seg_out NULL to fill `info`, then again with arrays of info->n_univ and
+ * info->n_seg entries.  The tables must then be copied to device memory.
+ * Replaces the reference's per-kernel set-up in start_kernel (e.g. np2.py:57-87,
+ * pc2.py:99-145); the work list has no reference counterpart.
+ */
+int grav_plan(int32_t n_univ, const int32_t* n, const double* T, const grav_tile* tile,
+	grav_plan_info* info, grav_univ_desc* univ_out, grav_seg_desc* seg_out);
+
+/* Bytes of the padded stage-1 position array for `mode` and `n_pad_total` rows. */
+int64_t grav_pos_bytes(int mode, int64_t n_pad_total);
+
+/* Bytes of the FP64 partial-sum buffer for a plan. */
+int64_t grav_part_bytes(const grav_plan_info* info);
+
+/* r^2 floor for the FP32 modes: the smallest value that keeps G*m * r^-3 finite in
+ * FP32 for the largest G*m.  It is far below the FP32 resolution of any separation
+ * larger than ~1e-7 of the body coordinates, so it does not act as softening. */
+float grav_eps2(double max_gm);
+
+/* ---- stages (device work, asynchronous on `stream`) ---------------------------- */
+
+/* Refresh the padded stage-1 positions from r (after r was written by the host). */
+int grav_prepare(const grav_batch* b, void* stream);
+
+/*
+ * Stage 1: FP64 partial sums of the accelerations into b->part.
+ * Replaces universe_base.step_stage1 (_base_.py:147-150) as realised by
+ * np1.update_pair/step_stage1 (np1.py:81-108), c1a's step_stage1
+ * (_lib1_/lib.c:52-126) and pc2.update_all (pc2.py:59-91).
+ */
+int grav_stage1(const grav_batch* b, void* stream);
+
+/*
+ * Stage 2: sum the partials (FP64), optionally write a_out, optionally integrate
+ * (v = a*T + v; r = v*T + r in FP64, no fused multiply-add, as _base_.py:58-62 and
+ * np2.py:110-115), then refresh the padded stage-1 positions.
+ * Replaces universe_base.step_stage2 (_base_.py:152-156) / np2.step_stage2.
+ */
+int grav_stage2(const grav_batch* b, int flags, void* stream);
+
+/* Stage 1 then stage 2 with `flags` (one full step when GRAV_S2_INTEGRATE).
+ * Replaces universe_base.step's stage 1 and stage 2 calls (_base_.py:143-144). */
+int grav_step(const grav_batch* b, int flags, void* stream);
+
+/* ---- measurement ------------------------------------------------------------------ */
+
+/* FP32 FMA throughput probe: `blocks` CTAs of 256 threads, each thread 8 independent
+ * FMA chains of 16*iters FMAs; writes blocks*256 floats to `out`.  Timed by the caller,
+ * it gives the FP32 peak (2 FLOP per FMA) the stage-1 roofline is quoted against.
+ * No reference counterpart (the reference times wall clock only, lib/timing.py:41-78). */
+int grav_fp32_peak_probe(float* out, int32_t blocks, int32_t iters, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GRAVITATION_GB300_H */

@@ -1,0 +1,118 @@
+"""Build recipe for the CPU oracle (test infrastructure only).
+
+Builds, with gcc, next to this file:
+  liboracle.so  -- oracle.c: FP64 all-pairs oracle, FP64 stage 2, energy, adjoint check
+  libport.so    -- ref_port.c: portable restatement of the reference's fastest CPU
+                   stage 1 (the timed CPU baseline)
+and, only where the reference tree is present (this is never the case on the GPU
+host), compiles the reference's own sources where they lie, into ``oracle/_ref/``:
+  _ref/lib1.so  -- gravitation/kernel/_lib1_/lib.c (the c1a kernel), with the
+                   reference's own flags (setup.py:82-99)
+  _ref/cy4/     -- gravitation/kernel/cy4/core.pyx through Cython (setup.py:73-78)
+The reference's _lib4_/lib.c (c4a/c4b) is not built: it includes x86 SSE headers
+(lib.c:39) and GCC 13 rejects its OpenMP data-sharing clause (lib.c:179-182).
+
+Usage: ``python oracle/build.py`` or ``oracle.build.build_all()``.
+"""
+
+import os
+import platform
+import shutil
+import subprocess
+import sys
+import sysconfig
+import tempfile
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_ROOT = os.environ.get('GRAVITATION_REFERENCE', '/root/reference')
+REF_KERNEL = os.path.join(REF_ROOT, 'src', 'gravitation', 'kernel')
+
+
+def _run(cmd):
+    subprocess.run(cmd, check=True)
+
+
+def _newer(target, *sources):
+    if not os.path.exists(target):
+        return False
+    t = os.path.getmtime(target)
+    return all(os.path.getmtime(s) <= t for s in sources)
+
+
+def build_oracle(force=False):
+    out = os.path.join(HERE, 'liboracle.so')
+    src = os.path.join(HERE, 'oracle.c')
+    if force or not _newer(out, src):
+        _run(['gcc', '-O2', '-fPIC', '-shared', '-fopenmp', '-ffp-contract=off',
+              '-std=gnu11', '-Wall', src, '-o', out, '-lm'])
+    return out
+
+
+def build_port(force=False):
+    out = os.path.join(HERE, 'libport.so')
+    src = os.path.join(HERE, 'ref_port.c')
+    if force or not _newer(out, src):
+        # the reference's own optimisation flags (setup.py:103-118) minus the
+        # x86-only -march=native / -mfpmath=sse
+        _run(['gcc', '-O3', '-ffast-math', '-fPIC', '-shared', '-fopenmp',
+              '-std=gnu11', '-Wall', src, '-o', out, '-lm'])
+    return out
+
+
+def reference_present():
+    return os.path.isfile(os.path.join(REF_KERNEL, '_base_.py'))
+
+
+def build_reference(force=False):
+    """Compile the reference's c1a C kernel and cy4 Cython kernel into oracle/_ref/.
+
+    Returns a dict name -> path (or an error string) for what was attempted.
+    """
+    result = {}
+    if not reference_present():
+        return result
+    refdir = os.path.join(HERE, '_ref')
+    os.makedirs(refdir, exist_ok=True)
+    lib1_src = os.path.join(REF_KERNEL, '_lib1_', 'lib.c')
+    lib1_out = os.path.join(refdir, 'lib1.so')
+    try:
+        if force or not _newer(lib1_out, lib1_src):
+            flags = ['-std=gnu11', '-fPIC', '-O3', '-ffast-math', '-Wall']
+            if platform.machine() in ('x86_64', 'AMD64'):
+                flags += ['-march=native', '-mtune=native', '-mfpmath=sse']
+            _run(['gcc'] + flags + ['-shared', lib1_src, '-o', lib1_out, '-lm'])
+        result['lib1'] = lib1_out
+    except (subprocess.CalledProcessError, OSError) as e:
+        result['lib1'] = 'unbuildable: %s' % e
+    cy4_src = os.path.join(REF_KERNEL, 'cy4', 'core.pyx')
+    cy4_dir = os.path.join(refdir, 'cy4')
+    suffix = sysconfig.get_config_var('EXT_SUFFIX')
+    cy4_out = os.path.join(cy4_dir, 'core' + suffix)
+    try:
+        if force or not _newer(cy4_out, cy4_src):
+            os.makedirs(cy4_dir, exist_ok=True)
+            with tempfile.TemporaryDirectory() as tmp:
+                c_file = os.path.join(tmp, 'core.c')
+                _run([sys.executable, '-m', 'cython', '-3', cy4_src, '-o', c_file])
+                inc = sysconfig.get_paths()['include']
+                _run(['gcc', '-O3', '-fPIC', '-shared', '-fopenmp', '-I', inc,
+                      c_file, '-o', cy4_out, '-lm'])
+        result['cy4'] = cy4_out
+    except (subprocess.CalledProcessError, OSError) as e:
+        result['cy4'] = 'unbuildable: %s' % e
+    return result
+
+
+def build_all(force=False):
+    out = {'oracle': build_oracle(force), 'port': build_port(force)}
+    out.update(build_reference(force))
+    return out
+
+
+def clean_reference():
+    shutil.rmtree(os.path.join(HERE, '_ref'), ignore_errors=True)
+
+
+if __name__ == '__main__':
+    for k, v in build_all(force='--force' in sys.argv).items():
+        print(k, v)

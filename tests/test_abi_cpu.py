@@ -1,0 +1,175 @@
+"""CPU tests of the C ABI: the library loads and exports every symbol declared in
+include/*.h, the host-side planner is correct (checked by walking the persistent
+kernel's work assignment in Python), and invalid arguments are rejected on the host
+before anything reaches a GPU."""
+
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+from gravitation_gb300 import _lib, build as gbuild
+from gravitation_gb300.engine import make_plan
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope='module')
+def L():
+    gbuild.build()
+    return _lib.load()
+
+
+def header_functions():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, 'include', '*.h')):
+        src = open(h).read()
+        src = re.sub(r'/\*.*?\*/', '', src, flags=re.S)
+        for m in re.finditer(r'^[A-Za-z_][\w \*]*?\b(grav_\w+)\s*\(', src, flags=re.M):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_header_symbols_exported(L):
+    names = header_functions()
+    assert len(names) >= 10
+    for name in names:
+        assert hasattr(L, name), 'symbol %s declared in include/ but not exported' % name
+    # and the Python binding declares every one of them
+    assert set(names) <= set(_lib.declared_symbols())
+
+
+def test_abi_version(L):
+    assert L.grav_abi_version() == _lib.GRAV_ABI_VERSION
+
+
+def simulate_kernel(info, univ, seg, jtile):
+    """Python walk of the persistent stage-1 kernel's assignment (stage1_f32.cu):
+    returns (unit -> CTA) coverage and the slots each CTA writes."""
+    U, G = info.n_units, info.grid
+    segs = [seg[i] for i in range(info.n_seg)]
+    begins = [s.unit_begin for s in segs]
+    covered = np.zeros(U, dtype=np.int64)
+    slots_written = {}
+    for c in range(G):
+        ub, ue = c * U // G, (c + 1) * U // G
+        assert ub < ue
+        # last segment with unit_begin <= ub
+        s = max(i for i, b in enumerate(begins) if b <= ub)
+        while ub < ue and s < len(segs):
+            S = segs[s]
+            if S.n_units == 0 or S.unit_begin + S.n_units <= ub:
+                s += 1
+                continue
+            jt0 = ub - S.unit_begin
+            jt1 = min(ue - S.unit_begin, S.n_units)
+            covered[S.unit_begin + jt0:S.unit_begin + jt1] += 1
+            slot = S.slot_base + (c - S.cta_first)
+            assert 0 <= c - S.cta_first < S.nslots
+            assert slot not in slots_written
+            slots_written[slot] = (s, c)
+            ub = S.unit_begin + jt1
+            s += 1
+    return covered, slots_written
+
+
+@pytest.mark.parametrize('sizes,tile', [
+    ([1], (1, 128, 128, 8)),
+    ([1000], (4, 128, 256, 300)),
+    ([65536], (4, 128, 256, 608)),
+    ([5, 0, 300, 129, 2048], (2, 128, 128, 40)),
+    ([64, 16384, 77, 1000, 3000], (4, 256, 256, 1216)),
+    ([3], (8, 256, 256, 5000)),
+])
+def test_plan_covers_every_unit_once(L, sizes, tile):
+    t = _lib.Tile(*tile)
+    info, univ, seg = make_plan(sizes, 1.0, t)
+    itile = t.bpt * t.threads
+    assert info.itile == itile and info.pad_unit == max(itile, t.jtile)
+    assert info.n_bodies == sum(sizes)
+    assert info.n_pad_total == info.n_seg * itile
+    assert info.grid == min(t.grid, info.n_units)
+    # universes: padded, aligned, contiguous
+    pad = 0
+    for u, n in enumerate(sizes):
+        d = univ[u]
+        assert d.n == n and d.pad_off == pad and d.pad_off % info.pad_unit == 0
+        assert d.n_jtiles == -(-n // t.jtile)
+        pad += -(-n // info.pad_unit) * info.pad_unit
+    assert pad == info.n_pad_total
+    # every i-tile of real bodies has one unit per j-tile; pure padding tiles have none
+    units = 0
+    for s in range(info.n_seg):
+        S = seg[s]
+        assert S.unit_begin == units
+        n = sizes[S.u]
+        assert S.n_units == (univ[S.u].n_jtiles if S.il0 < n else 0)
+        units += S.n_units
+    assert units == info.n_units
+    if info.n_units:
+        covered, slots = simulate_kernel(info, univ, seg, t.jtile)
+        assert np.all(covered == 1)
+        assert sorted(slots) == list(range(info.n_slots))
+
+
+def test_plan_rejects_bad_input(L):
+    info = _lib.PlanInfo()
+    n = (ctypes.c_int32 * 2)(5, -1)
+    t = _lib.Tile(4, 128, 256, 10)
+    assert L.grav_plan(2, n, None, ctypes.byref(t), ctypes.byref(info), None, None) == _lib.GRAV_E_ARG
+    assert 'n[1]' in _lib.last_error()
+    t = _lib.Tile(3, 128, 256, 10)
+    n = (ctypes.c_int32 * 1)(5)
+    assert L.grav_plan(1, n, None, ctypes.byref(t), ctypes.byref(info), None, None) == _lib.GRAV_E_ARG
+    assert L.grav_plan(1, n, None, None, ctypes.byref(info), None, None) == _lib.GRAV_E_ARG
+
+
+def test_stage_calls_reject_bad_batch_on_host(L):
+    # none of these reach the GPU: validation fails first
+    assert L.grav_stage1(None, None) == _lib.GRAV_E_ARG
+    b = _lib.Batch()
+    b.mode = 7
+    assert L.grav_stage1(ctypes.byref(b), None) == _lib.GRAV_E_ARG
+    assert 'mode' in _lib.last_error()
+    b.mode = _lib.GRAV_MODE_FP32
+    b.tile = _lib.Tile(4, 128, 256, 1)
+    b.n_seg = 2
+    b.n_pad_total = 1000          # != n_seg * itile
+    assert L.grav_stage2(ctypes.byref(b), 1, None) == _lib.GRAV_E_ARG
+    b.n_pad_total = 1024
+    b.n_univ = 1
+    assert L.grav_stage1(ctypes.byref(b), None) == _lib.GRAV_E_ARG   # NULL pointers
+    assert L.grav_stage2(ctypes.byref(b), 0x40, None) == _lib.GRAV_E_ARG
+
+
+def test_tile_table(L):
+    for mode in ('fp32', 'fp32c', 'fp64'):
+        m = _lib.MODES[mode]
+        n = L.grav_tile_list(m, None, 0)
+        assert n > 0
+        arr = (_lib.Tile * n)()
+        assert L.grav_tile_list(m, arr, n) == n
+        for t in arr:
+            assert L.grav_tile_supported(m, ctypes.byref(t)) == 1
+    assert L.grav_tile_supported(0, ctypes.byref(_lib.Tile(3, 100, 7, 1))) == 0
+
+
+def test_eps2_keeps_self_term_finite(L):
+    for gm in (0.0, 1e-12, 6.7e-9, 1.0, 1e6, 1e12):
+        e = L.grav_eps2(gm)
+        assert e > 1.17549435e-38                 # a normal FP32 number
+        inv = np.float32(1.0) / np.sqrt(np.float32(e))
+        w = np.float32(gm) * inv * inv * inv
+        assert np.isfinite(w)
+    # far below the FP32 resolution of a unit-size separation
+    assert L.grav_eps2(1.0) < 1e-20
+
+
+def test_pos_and_part_bytes(L):
+    assert L.grav_pos_bytes(0, 1024) == 16 * 1024
+    assert L.grav_pos_bytes(1, 1024) == 32 * 1024
+    assert L.grav_pos_bytes(2, 1024) == 32 * 1024
+    assert L.grav_pos_bytes(9, 1024) < 0

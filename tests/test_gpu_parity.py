@@ -1,0 +1,227 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the CPU oracle and the
+reference's golden vectors.
+
+Tolerances (relative per-body acceleration error |a - a_ref| / |a_ref|):
+  fp32   1e-5 against the FP64 oracle evaluated on the FP32-rounded positions the
+         kernel reads (arithmetic error), as the reference's own FP32 kernels
+         (np1/np2) are measured from identical states
+  fp32c  1e-5 against the FP64 oracle on the FP64 state itself
+  fp64   1e-12 against the FP64 oracle on the FP64 state
+Stage 2 is bit-exact against the FP64 update of _base_.py:58-62.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from gravitation_gb300 import _lib
+from gravitation_gb300.engine import Engine, tile_list
+from gravitation_gb300.scenarios import G_DEFAULT, uniform_cube, plummer_pair
+
+pytestmark = pytest.mark.gpu
+
+TOL = {'fp32': 1e-5, 'fp32c': 1e-5, 'fp64': 1e-12}
+
+
+def r32(r):
+    return np.asarray(r, dtype=np.float64).astype(np.float32).astype(np.float64)
+
+
+def oracle_accel(mode, r, m, G, rows=None):
+    """FP64 oracle on the state the mode is compared against (see module doc)."""
+    if mode == 'fp32':
+        gm32 = (G * np.asarray(m)).astype(np.float32).astype(np.float64)
+        return oracle.accel_fp64(r32(r), gm32, 1.0, rows=rows, coincident=True)
+    return oracle.accel_fp64(r, G * np.asarray(m), 1.0, rows=rows, coincident=True)
+
+
+def engine_forces(mode, r, v, m, G=G_DEFAULT, tile=None):
+    eng = Engine([len(m)], 1e3, mode=mode, tile=tile)
+    eng.set_state(r, v, G * np.asarray(m))
+    a = eng.forces().cpu().numpy()
+    eng.raise_on_device_error()
+    return a, eng
+
+
+@pytest.mark.parametrize('mode', ['fp32', 'fp32c', 'fp64'])
+@pytest.mark.parametrize('n', [1, 2, 3, 31, 33, 127, 129, 257, 1000])
+def test_forces_small_n(gpu, mode, n):
+    r, v, m = uniform_cube(n, seed=100 + n)
+    a, _ = engine_forces(mode, r, v, m)
+    ref = oracle_accel(mode, r, m, G_DEFAULT)
+    if n == 1:
+        assert np.all(a == 0.0)
+        return
+    err = oracle.rel_err_per_body(a, ref)
+    assert err.max() < TOL[mode], (mode, n, err.max())
+
+
+@pytest.mark.parametrize('mode', ['fp32', 'fp32c', 'fp64'])
+def test_every_tile_shape(gpu, mode):
+    n = 777
+    r, v, m = uniform_cube(n, seed=7)
+    ref = oracle_accel(mode, r, m, G_DEFAULT)
+    for t in tile_list(mode):
+        for grid in (1, 3, 1000):
+            a, _ = engine_forces(mode, r, v, m, tile=_lib.Tile(t.bpt, t.threads, t.jtile, grid))
+            err = oracle.rel_err_per_body(a, ref).max()
+            assert err < TOL[mode], (mode, t, grid, err)
+
+
+def test_np1_golden_fp32(gpu, golden):
+    """The reference's np1 FP32 per-step accelerations, from the same state."""
+    G = float(golden['G_scaled'])
+    r0, v0, m = golden['c0_r0'], golden['c0_v0'], golden['c0_m']
+    a, _ = engine_forces('fp32', r0, v0, m, G)
+    ref64 = oracle_accel('fp32', r0, m, G)
+    assert oracle.rel_err_per_body(a, ref64).max() < 1e-5
+    assert oracle.rel_err_per_body(a, golden['np1_f32_a'][0]).max() < 2e-5
+
+
+def test_np1_golden_trajectory_fp32(gpu, golden):
+    """10 steps with FP32 stage 1 and FP64 stage 2 -- the same split as np1 with the
+    base class's stage 2 -- against np1's states and accelerations."""
+    G, T = float(golden['G_scaled']), float(golden['T'])
+    r0, v0, m = golden['c0_r0'], golden['c0_v0'], golden['c0_m']
+    eng = Engine([len(m)], T, mode='fp32')
+    eng.set_state(r0, v0, G * m)
+    for k in range(10):
+        eng.step(1, write_a=True)
+        a = eng.a[:len(m), :3].cpu().numpy()
+        assert oracle.rel_err_per_body(a, golden['np1_f32_a'][k]).max() < 2e-5, k
+    r = eng.r[:len(m), :3].cpu().numpy()
+    v = eng.v[:len(m), :3].cpu().numpy()
+    assert np.max(np.abs(r - golden['np1_f32_r10']) / np.abs(golden['np1_f32_r10'])) < 1e-12
+    assert np.max(np.abs(v - golden['np1_f32_v10'])) < 1e-9
+
+
+def test_np1_golden_trajectory_fp64(gpu, golden):
+    G, T = float(golden['G_scaled']), float(golden['T'])
+    r0, v0, m = golden['c0_r0'], golden['c0_v0'], golden['c0_m']
+    eng = Engine([len(m)], T, mode='fp64')
+    eng.set_state(r0, v0, G * m)
+    eng.step(1, write_a=True)
+    assert oracle.rel_err_per_body(eng.a[:len(m), :3].cpu().numpy(),
+                                   golden['np1_f64_a0']).max() < 1e-12
+    eng.step(9)
+    r = eng.r[:len(m), :3].cpu().numpy()
+    assert np.max(np.abs(r - golden['np1_f64_r10']) / np.abs(golden['np1_f64_r10'])) < 1e-13
+    eng.raise_on_device_error()
+
+
+def test_py1_golden_fp64(gpu, golden):
+    a, _ = engine_forces('fp64', golden['py1_r0'], golden['py1_v0'], golden['py1_m'])
+    assert oracle.rel_err_per_body(a, golden['py1_a0']).max() < 1e-12
+
+
+@pytest.mark.parametrize('mode', ['fp32', 'fp64'])
+def test_stage2_bit_exact(gpu, mode):
+    """Given the accelerations, stage 2 equals v = a*T + v ; r = v*T + r in FP64."""
+    n = 3000
+    r, v, m = uniform_cube(n, seed=21)
+    eng = Engine([n], 1e3, mode=mode)
+    eng.set_state(r, v, G_DEFAULT * m)
+    a = eng.forces().cpu().numpy().copy()
+    eng.stage2(_lib.GRAV_S2_INTEGRATE)
+    r_exp, v_exp = oracle.stage2_fp64(r, v, a, 1e3)
+    assert np.array_equal(eng.v[:n, :3].cpu().numpy(), v_exp)
+    assert np.array_equal(eng.r[:n, :3].cpu().numpy(), r_exp)
+
+
+def test_full_size_sampled_65536(gpu):
+    """N = 65536: sampled bodies against the FP64 oracle, all three modes."""
+    n = 65536
+    r, v, m = uniform_cube(n, seed=0)
+    rows = np.random.default_rng(9).choice(n, 192, replace=False)
+    for mode in ('fp32', 'fp32c'):
+        a, _ = engine_forces(mode, r, v, m)
+        ref = oracle_accel(mode, r, m, G_DEFAULT, rows=rows)
+        err = oracle.rel_err_per_body(a[rows], ref)
+        assert err.max() < 1e-5, (mode, err.max())
+    # the plain mode's error on the FP64 state itself includes the rounding of the
+    # positions to FP32; it is reported, bounded loosely here
+    a, _ = engine_forces('fp32', r, v, m)
+    ref = oracle.accel_fp64(r, G_DEFAULT * m, 1.0, rows=rows)
+    assert oracle.rel_err_per_body(a[rows], ref).max() < 2e-4
+
+
+def test_size_independent_properties_65536(gpu):
+    n = 65536
+    r, v, m = uniform_cube(n, seed=0)
+    a1, eng = engine_forces('fp32', r, v, m)
+    a2 = eng.forces().cpu().numpy()
+    assert np.array_equal(a1, a2)                         # deterministic
+    # momentum: sum_i m_i a_i = 0 (pairwise antisymmetry), relative to sum m|a|
+    p = (m[:, None] * a1).sum(0)
+    assert np.linalg.norm(p) < 1e-6 * (m * np.linalg.norm(a1, axis=1)).sum()
+    # tile shape does not change the answer beyond FP32 rounding
+    t = tile_list('fp32')[0]
+    a3, _ = engine_forces('fp32', r, v, m, tile=_lib.Tile(t.bpt, t.threads, t.jtile, 97))
+    assert oracle.rel_err_per_body(a3, a1).max() < 2e-6
+
+
+def test_plummer_pair_precision_modes(gpu):
+    """Clustered input far from the origin: fp32c and fp64 hold their bounds on the
+    FP64 state; plain fp32 holds its bound on the positions it reads."""
+    n = 4096
+    r, v, m = plummer_pair(n, seed=2)
+    rows = np.arange(0, n, 16)
+    for mode in ('fp32', 'fp32c', 'fp64'):
+        a, _ = engine_forces(mode, r, v, m)
+        ref = oracle_accel(mode, r, m, G_DEFAULT, rows=rows)
+        err = oracle.rel_err_per_body(a[rows], ref).max()
+        assert err < TOL[mode], (mode, err)
+
+
+def test_edge_cases(gpu):
+    # two bodies: analytic
+    r = np.array([[0.0, 0, 0], [3.0, 4.0, 0]])
+    m = np.array([2.0, 5.0]) / G_DEFAULT
+    for mode in ('fp32', 'fp64'):
+        a, _ = engine_forces(mode, r, np.zeros((2, 3)), m)
+        d = np.array([3.0, 4.0, 0]) / 125.0
+        assert np.allclose(a[0], 5.0 * d, rtol=1e-6) and np.allclose(a[1], -2.0 * d, rtol=1e-6)
+    # coincident bodies exert no force on each other (the reference gives inf/nan)
+    r = np.array([[0.0, 0, 0], [1.0, 0, 0], [1.0, 0, 0]])
+    m = np.ones(3) / G_DEFAULT
+    for mode in ('fp32', 'fp32c', 'fp64'):
+        a, _ = engine_forces(mode, r, np.zeros((3, 3)), m)
+        assert np.all(np.isfinite(a))
+        assert np.allclose(a[1], [-1.0, 0, 0], rtol=1e-6)
+        assert np.allclose(a[0], [2.0, 0, 0], rtol=1e-6)
+    # massless bodies feel forces but exert none
+    r, v, m = uniform_cube(100, seed=3)
+    m[::3] = 0.0
+    a, _ = engine_forces('fp64', r, v, m)
+    ref = oracle.accel_fp64(r, G_DEFAULT * m, 1.0)
+    assert oracle.rel_err_per_body(a, ref).max() < 1e-12
+    # negative masses are rejected on the host
+    with pytest.raises(ValueError):
+        engine_forces('fp32', r, v, -m)
+
+
+def test_batched_matches_single(gpu):
+    """Several universes in one persistent launch == each universe alone."""
+    sizes = [64, 1000, 3, 4096, 517]
+    rs, vs, ms = zip(*[uniform_cube(n, seed=50 + i) for i, n in enumerate(sizes)])
+    for mode in ('fp32', 'fp64'):
+        eng = Engine(sizes, [1e3] * len(sizes), mode=mode)
+        eng.set_state(np.concatenate(rs), np.concatenate(vs), G_DEFAULT * np.concatenate(ms))
+        a = eng.forces().cpu().numpy()
+        for u, n in enumerate(sizes):
+            ref = oracle_accel(mode, rs[u], ms[u], G_DEFAULT)
+            err = oracle.rel_err_per_body(a[eng.universe_slice(u)], ref).max()
+            assert err < TOL[mode], (mode, u, err)
+        eng.step(3)
+        eng.raise_on_device_error()
+
+
+def test_context_usable_after_many_launches(gpu):
+    r, v, m = uniform_cube(2048, seed=1)
+    eng = Engine([2048], 1e3, mode='fp32')
+    eng.set_state(r, v, G_DEFAULT * m)
+    eng.step(50)
+    torch.cuda.synchronize()
+    eng.raise_on_device_error()
+    assert torch.isfinite(eng.r).all()
