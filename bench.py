@@ -54,6 +54,11 @@ def parse():
                     help='target seconds per CPU-baseline sample run (3 runs)')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-e2e', action='store_true')
+    ap.add_argument('--profile', action='store_true',
+                    help='only set up the workload and run --steps stage-1 launches '
+                         '(for ncu captures); prints nothing on success')
+    ap.add_argument('--tile', default=None,
+                    help='force the stage-1 tile as bpt,threads,jtile (default: autotuned)')
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
     return a
@@ -262,9 +267,19 @@ def run_ours(args):
     n = args.n
     r, v, m = uniform_cube(n, seed=0)
     gm = G_DEFAULT * m
-    eng = Engine([n], T_DEFAULT, mode=args.mode, tuner=default_tuner(), device=local)
+    if args.tile:
+        bpt, thr, jt = (int(x) for x in args.tile.split(','))
+        eng = Engine([n], T_DEFAULT, mode=args.mode, tile=_lib.Tile(bpt, thr, jt, 0), device=local)
+    else:
+        eng = Engine([n], T_DEFAULT, mode=args.mode, tuner=default_tuner(), device=local)
     eng.set_state(r, v, gm)
     stream = torch.cuda.current_stream(device)
+    if args.profile:
+        for _ in range(args.warmup + args.steps):
+            eng.stage1()
+        torch.cuda.synchronize()
+        eng.raise_on_device_error()
+        return 0
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=device)
 
     # accuracy on sampled bodies before timing (FP64 oracle on the host)

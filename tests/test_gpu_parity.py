@@ -87,13 +87,27 @@ def test_np1_golden_trajectory_fp32(gpu, golden):
     eng = Engine([len(m)], T, mode='fp32')
     eng.set_state(r0, v0, G * m)
     for k in range(10):
+        rk = eng.r[:len(m), :3].cpu().numpy()
         eng.step(1, write_a=True)
         a = eng.a[:len(m), :3].cpu().numpy()
-        assert oracle.rel_err_per_body(a, golden['np1_f32_a'][k]).max() < 2e-5, k
+        # ours against the FP64 oracle on the positions stage 1 reads
+        ref = oracle_accel('fp32', rk, m, G)
+        assert oracle.rel_err_per_body(a, ref).max() < 1e-5, k
+        # and against np1's own FP32 result: np1 itself is up to ~2e-5 away from the
+        # FP64 oracle on some bodies, so agreement is bounded by np1's own error + 1e-5
+        e_np1 = oracle.rel_err_per_body(golden['np1_f32_a'][k], ref)
+        e_pair = oracle.rel_err_per_body(a, golden['np1_f32_a'][k])
+        assert np.all(e_pair <= e_np1 * 1.01 + 1e-5), k
     r = eng.r[:len(m), :3].cpu().numpy()
     v = eng.v[:len(m), :3].cpu().numpy()
-    assert np.max(np.abs(r - golden['np1_f32_r10']) / np.abs(golden['np1_f32_r10'])) < 1e-12
-    assert np.max(np.abs(v - golden['np1_f32_v10'])) < 1e-9
+    # FP64 integration: the FP32 force error (~1e-6 of a) moves r by ~1e-6 a T^2,
+    # far below the positions' size
+    r64, v64 = oracle.rollout_fp64(r0, v0, m, G, T, 10)
+    assert np.max(np.abs(r - r64) / np.abs(r64)) < 1e-12
+    assert np.max(np.abs(v - v64)) < 1e-12
+    # np1's state: its stage 2 runs on numpy float32 scalars (pm._a holds float32
+    # after np1.py:107-108, so a*T + v stays float32), i.e. FP32 integration
+    assert np.max(np.abs(r - golden['np1_f32_r10']) / np.abs(golden['np1_f32_r10'])) < 1e-4
 
 
 def test_np1_golden_trajectory_fp64(gpu, golden):
