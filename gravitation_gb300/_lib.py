@@ -103,7 +103,10 @@ _DECLS = {
     'grav_step': (ctypes.c_int, [_P(Batch), ctypes.c_int, ctypes.c_void_p]),
     'grav_fp32_peak_probe': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                                             ctypes.c_void_p]),
+    'grav_forces_noalloc': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                           ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]),
 }
+GRAV_NOALLOC_MAX_N = 16384
 
 _lock = threading.Lock()
 _lib = None

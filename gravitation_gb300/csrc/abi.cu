@@ -82,6 +82,14 @@ int check_batch(const grav_batch* b)
 
 }  // namespace
 
+namespace grav {
+// Message for grav_last_error() from other translation units (failure paths only).
+int record_error(int code, const char* msg)
+{
+	return fail(code, "%s", msg);
+}
+}  // namespace grav
+
 extern "C" {
 
 int grav_abi_version(void)

@@ -190,6 +190,33 @@ int grav_stage2(const grav_batch* b, int flags, void* stream);
  * Replaces universe_base.step's stage 1 and stage 2 calls (_base_.py:143-144). */
 int grav_step(const grav_batch* b, int flags, void* stream);
 
+/* ---- allocation-free variant ------------------------------------------------------- */
+
+/* Largest universe grav_forces_noalloc accepts. */
+#define GRAV_NOALLOC_MAX_N 16384
+
+/*
+ * Accelerations of one universe of n <= GRAV_NOALLOC_MAX_N bodies for callers that
+ * cannot allocate device memory where they need forces (code inside another
+ * framework's memory pool, threads that must not enter the CUDA allocator while other
+ * work is captured or timed, hosts that reserve all device memory up front).
+ * Inputs: r, n x 4 doubles (x, y, z, G*m) on the device; max_gm = the largest G*m
+ * (sets the FP32 r^2 floor, see grav_eps2).  Output: a, n x 4 doubles (ax, ay, az, 0).
+ * err: optional device int (GRAV_DEV_* written by the kernels; NULL = internal).
+ * Same arithmetic as grav_stage1 + grav_stage2(GRAV_S2_WRITE_A) in GRAV_MODE_FP32, on a
+ * fixed tile (2 bodies/thread, 128 threads, 128-body j-tiles).
+ * It calls no cudaMalloc/cudaFree or other allocating routine: its scratch (plan
+ * tables, padded positions, FP64 partial sums, error flag) is one file-scope device
+ * array of about 3.8 MB that every GPU loading the library holds until exit.  The first
+ * call on each device, with that device current, looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.  Every call
+ * shares the array: calls whose work overlaps on the GPU race.  n above the limit is
+ * rejected with GRAV_E_SIZE.  Failures are described by grav_last_error().
+ * No counterpart in the reference.
+ */
+int grav_forces_noalloc(const double* r, double* a, int32_t n, double max_gm, int32_t* err,
+	void* stream);
+
 /* ---- measurement ------------------------------------------------------------------ */
 
 /* FP32 FMA throughput probe: `blocks` CTAs of 256 threads, each thread 8 independent
