@@ -1,0 +1,138 @@
+"""CPU tests of the drop-in boundary: the kernel package's metadata is what the
+reference's AST loader reads, the reference's own inventory discovers and imports it
+from a copy of the reference tree, and the stand-alone universe_base restatement
+behaves like the reference's class (scaling, state machine, default stage 2)."""
+
+import ast
+import os
+import shutil
+import subprocess
+import sys
+import textwrap
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GB1 = os.path.join(ROOT, 'gravitation_gb300', 'kernel', 'gb1')
+REF = os.environ.get('GRAVITATION_REFERENCE', '/root/reference')
+REF_SRC = os.path.join(REF, 'src')
+META = ('longname', 'version', 'description', 'requirements', 'externalrequirements',
+        'interpreters', 'parallel', 'license', 'authors')
+
+
+def test_metadata_is_literal():
+    tree = ast.parse(open(os.path.join(GB1, '__init__.py')).read())
+    found = {}
+    for item in tree.body:
+        if isinstance(item, ast.Assign):
+            for t in item.targets:
+                # the reference's loader reads target.id of every top-level assignment
+                assert isinstance(t, ast.Name)
+                found[t.id] = ast.literal_eval(item.value)
+    for k in META:
+        assert '__%s__' % k in found, k
+    assert found['__parallel__'] is True
+    assert 'cuda' in found['__externalrequirements__']
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_SRC), reason='reference tree not present')
+def test_reference_inventory_discovers_gb1(tmp_path):
+    src = tmp_path / 'src'
+    shutil.copytree(os.path.join(REF_SRC, 'gravitation'), src / 'gravitation',
+                    ignore=shutil.ignore_patterns('__pycache__', '*.so'))
+    shutil.copytree(GB1, src / 'gravitation' / 'kernel' / 'gb1',
+                    ignore=shutil.ignore_patterns('__pycache__'))
+    script = textwrap.dedent('''
+        import sys, warnings
+        warnings.simplefilter("ignore", DeprecationWarning)
+        sys.path[:0] = [%r, %r]
+        from gravitation.lib.load import inventory
+        from gravitation.kernel._base_ import universe_base
+        k = inventory["gb1"]
+        k.load_meta()
+        assert k["longname"].startswith("gb300"), k["longname"]
+        assert k["name"] == "gb1"
+        k.load_module()
+        cls = k.get_class()
+        assert issubclass(cls, universe_base), cls.__mro__
+        assert cls.__module__ == "gravitation.kernel.gb1"
+        u = cls(T=2.0e12, scale_m=1e-30, scale_r=1e-10)
+        u.add_object(name="a", r=[1.0, 2.0, 3.0], v=[0.0, 0.0, 0.0], m=2e30)
+        assert u._G == 6.6740831e-11 * 1e-30 / 1e-30
+        print("OK", sorted(inventory.keys())[:3])
+    ''' % (str(src), ROOT))
+    res = subprocess.run([sys.executable, '-c', script], capture_output=True, text=True,
+                         timeout=300)
+    assert res.returncode == 0, res.stderr[-2000:]
+    assert 'OK' in res.stdout
+
+
+def _ref_base():
+    if not os.path.isdir(REF_SRC):
+        pytest.skip('reference tree not present')
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        '_ref_base_', os.path.join(REF_SRC, 'gravitation', 'kernel', '_base_.py'))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def test_base_restatement_matches_reference():
+    ref = _ref_base()
+    from gravitation_gb300.kernel import _base_ as ours
+    for kw in ({}, {'scale_m': 1e-30, 'scale_r': 1e-10, 'T': 2e12},
+               {'scale_m': 3.0, 'scale_r': 2.0, 'scale_off': True, 'foo': 1}):
+        a = ref.universe_base(**dict(kw))
+        b = ours.universe_base(**dict(kw))
+        assert a._G == b._G and a._T == b._T and a._meta == b._meta
+        for u in (a, b):
+            u.add_object(name='x', r=[1.0, 2.0, 3.0], v=[0.5, 0.0, -1.0], m=7.0)
+            u.add_object(name='y', r=[-1.0, 0.0, 3.0], v=[0.0, 0.0, 0.0], m=1.0, scale_off=True)
+        for pa, pb in zip(a, b):
+            assert pa._r == pb._r and pa._v == pb._v and pa._m == pb._m and pa._a == pb._a
+            assert str(pa) == str(pb)
+        # state machine
+        for u in (a, b):
+            with pytest.raises(SyntaxError):
+                u.step()
+            with pytest.raises(SyntaxError):
+                u.stop()
+            u.start()
+            with pytest.raises(SyntaxError):
+                u.start()
+            with pytest.raises(SyntaxError):
+                u.add_object(name='z', r=[0.0] * 3, v=[0.0] * 3, m=1.0)
+            with pytest.raises(NotImplementedError):
+                u.step()
+        # default stage 2 on identical accelerations
+        for u in (a, b):
+            for i, pm in enumerate(u):
+                pm._a[:] = [1e-3 * (i + 1), -2e-3, 3e-3]
+            u.step_stage2()
+            u.step_stage3()
+        for pa, pb in zip(a, b):
+            assert pa._r == pb._r and pa._v == pb._v and pa._a == pb._a
+        assert a._t == b._t
+        for u in (a, b):
+            u.stop()
+            with pytest.raises(SyntaxError):
+                u.stop()
+
+
+def test_default_stage2_matches_oracle():
+    import oracle
+    from gravitation_gb300.kernel._base_ import universe_base
+    rng = np.random.default_rng(2)
+    r, v, a = rng.normal(size=(5, 3)), rng.normal(size=(5, 3)), rng.normal(size=(5, 3))
+    u = universe_base(T=123.0)
+    for i in range(5):
+        u.add_object(name='b', r=list(r[i]), v=list(v[i]), m=1.0)
+    u.start()
+    for i, pm in enumerate(u):
+        pm._a[:] = list(a[i])
+    u.step_stage2()
+    r2, v2 = oracle.stage2_fp64(r, v, a, 123.0)
+    assert np.array_equal(np.array([pm._r for pm in u]), r2)
+    assert np.array_equal(np.array([pm._v for pm in u]), v2)
