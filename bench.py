@@ -54,6 +54,8 @@ def parse():
                     help='target seconds per CPU-baseline sample run (3 runs)')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-e2e', action='store_true')
+    ap.add_argument('--no-batched', action='store_true')
+    ap.add_argument('--no-adjoint', action='store_true')
     ap.add_argument('--profile', action='store_true',
                     help='only set up the workload and run --steps stage-1 launches '
                          '(for ncu captures); prints nothing on success')
@@ -334,6 +336,17 @@ def run_ours(args):
     if not args.no_e2e:
         e2e = run_e2e(args, r, v, m, local)
 
+    batched = None
+    if not args.no_batched:
+        from gravitation_gb300.workloads import run_batched
+        batched = run_batched(steps=100, warmup=args.warmup, mode=args.mode,
+                              tuner=default_tuner(), device=local)
+
+    adjoint = None
+    if not args.no_adjoint:
+        from gravitation_gb300.workloads import run_adjoint
+        adjoint = run_adjoint(tuner=default_tuner(), device=local)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cv, threads, sample = cpu_baseline_run(n, 0, args.cpu_seconds)
@@ -371,6 +384,8 @@ def run_ours(args):
         'gpu_launches': 2 * args.steps,
         'e2e': e2e,
         'cpu_baseline': cpu,
+        'batched': batched,
+        'adjoint': adjoint,
     }
     print(json.dumps(line))
     return 0

@@ -82,6 +82,11 @@ class Batch(ctypes.Structure):
                 ('err', ctypes.c_void_p)]
 
 
+class Adjoint(ctypes.Structure):
+    _fields_ = [('b', ctypes.POINTER(Batch)), ('gr', ctypes.c_void_p), ('gv', ctypes.c_void_p),
+                ('ggm', ctypes.c_void_p), ('upos', ctypes.c_void_p), ('part7', ctypes.c_void_p)]
+
+
 # ---- declarations -----------------------------------------------------------------
 _P = ctypes.POINTER
 _DECLS = {
@@ -103,6 +108,11 @@ _DECLS = {
     'grav_step': (ctypes.c_int, [_P(Batch), ctypes.c_int, ctypes.c_void_p]),
     'grav_fp32_peak_probe': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                                             ctypes.c_void_p]),
+    'grav_energy': (ctypes.c_int, [_P(Batch), ctypes.c_void_p, ctypes.c_void_p]),
+    'grav_adjoint_tile_supported': (ctypes.c_int, [_P(Tile)]),
+    'grav_adjoint_occupancy': (ctypes.c_int, [_P(Tile), _P(ctypes.c_int32)]),
+    'grav_adjoint_prepare': (ctypes.c_int, [_P(Adjoint), ctypes.c_void_p]),
+    'grav_adjoint_step': (ctypes.c_int, [_P(Adjoint), ctypes.c_void_p]),
     'grav_forces_noalloc': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
                                            ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]),
 }

@@ -1,0 +1,185 @@
+"""Differentiable rollout: K steps forward with FP64 checkpoints, discrete adjoint back.
+
+``rollout(r0, v0, m, G, T, steps, every)`` is a torch.autograd.Function: its forward
+runs ``steps`` GB300 steps (FP32 stage 1, FP64 stage 2) and keeps the FP64 state at
+the start of every ``every``-step segment; its backward sweeps the segments from last
+to first.  Each segment starts from the exact stored state at its end, reverses the
+update step by step in FP64 while the adjoint pair kernel recomputes stage 1 at each
+reconstructed position and applies the transposed stage 2 and stage 1 (see
+csrc/adjoint.cu).  Gradients are returned for the initial positions, velocities and
+masses.  Memory: one FP64 state per segment, no per-step storage.
+"""
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import check
+from .engine import Engine, device_info, make_plan, _ctypes_to_device
+
+ADJ_TILE = (2, 128, 128)
+
+
+class AdjointEngine:
+    """Buffers and plan of the backward sweep for a packed batch of universes."""
+
+    def __init__(self, sizes, T, device=None, tile=ADJ_TILE):
+        self.lib = _lib.load()
+        self.dev_info = device_info(device)
+        self.device = torch.device('cuda', self.dev_info.index)
+        self.sizes = [int(n) for n in sizes]
+        t = _lib.Tile(tile[0], tile[1], tile[2], 0)
+        if not self.lib.grav_adjoint_tile_supported(ctypes.byref(t)):
+            raise ValueError('no adjoint kernel for tile %r' % (tile,))
+        occ = ctypes.c_int32()
+        with torch.cuda.device(self.device):
+            check(self.lib.grav_adjoint_occupancy(ctypes.byref(t), ctypes.byref(occ)))
+        t.grid = self.dev_info.sm_count * max(occ.value, 1)
+        self.info, univ, seg = make_plan(self.sizes, T, t)
+        info, dev = self.info, self.device
+        self.univ_dev = _ctypes_to_device(univ, ctypes.sizeof(_lib.UnivDesc) * info.n_univ, dev)
+        self.seg_dev = _ctypes_to_device(seg, ctypes.sizeof(_lib.SegDesc) * info.n_seg, dev)
+        nb = max(info.n_bodies, 1)
+        f64 = dict(dtype=torch.float64, device=dev)
+        self.r = torch.zeros((nb, 4), **f64)
+        self.v = torch.zeros((nb, 4), **f64)
+        self.gr = torch.zeros((nb, 4), **f64)
+        self.gv = torch.zeros((nb, 4), **f64)
+        self.ggm = torch.zeros(nb, **f64)
+        self.pos = torch.zeros(max(info.n_pad_total, 1) * 4, dtype=torch.float32, device=dev)
+        self.upos = torch.zeros_like(self.pos)
+        self.part7 = torch.zeros(max(info.n_slots * 7 * info.itile, 1), **f64)
+        self.err = torch.zeros(1, dtype=torch.int32, device=dev)
+        b = _lib.Batch()
+        b.mode = _lib.GRAV_MODE_FP32
+        b.n_univ, b.n_seg, b.n_slots = info.n_univ, info.n_seg, info.n_slots
+        b.n_bodies, b.n_pad_total, b.n_units = info.n_bodies, info.n_pad_total, info.n_units
+        b.tile = _lib.Tile(t.bpt, t.threads, t.jtile, info.grid)
+        b.eps2 = 1e-30
+        b.univ, b.seg = self.univ_dev.data_ptr(), self.seg_dev.data_ptr()
+        b.r, b.v, b.pos = self.r.data_ptr(), self.v.data_ptr(), self.pos.data_ptr()
+        b.part, b.a_out, b.err = self.part7.data_ptr(), None, self.err.data_ptr()
+        self.batch = b
+        a = _lib.Adjoint()
+        a.b = ctypes.pointer(b)
+        a.gr, a.gv, a.ggm = self.gr.data_ptr(), self.gv.data_ptr(), self.ggm.data_ptr()
+        a.upos, a.part7 = self.upos.data_ptr(), self.part7.data_ptr()
+        self.adj = a
+        self._aref = ctypes.byref(a)
+
+    def _h(self, stream):
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        return ctypes.c_void_p(s.cuda_stream)
+
+    def set_state(self, r4, v4):
+        """State (FP64 rows x, y, z, G*m / vx, vy, vz, 0) the next step reverses from."""
+        self.r.copy_(r4)
+        self.v.copy_(v4)
+
+    def prepare(self, stream=None):
+        check(self.lib.grav_adjoint_prepare(self._aref, self._h(stream)))
+
+    def step(self, stream=None):
+        check(self.lib.grav_adjoint_step(self._aref, self._h(stream)))
+
+    def raise_on_device_error(self):
+        code = int(self.err.item())
+        if code != _lib.GRAV_DEV_OK:
+            self.err.zero_()
+            raise _lib.GravError(_lib.GRAV_E_CUDA, 'device error flag %d in the adjoint' % code)
+
+
+class Rollout:
+    """Forward engine + adjoint engine for one batch of universes (reusable)."""
+
+    def __init__(self, sizes, T, steps, every=32, device=None, fwd_tile=None, tuner=None):
+        self.sizes = [int(n) for n in sizes]
+        self.T = float(T)
+        self.steps = int(steps)
+        self.every = max(1, int(every))
+        self.fwd = Engine(self.sizes, self.T, mode='fp32', tile=fwd_tile, device=device,
+                          tuner=tuner)
+        self.adj = AdjointEngine(self.sizes, self.T, device=device)
+        self.checkpoints = []
+
+    def forward(self, r0, v0, gm, stream=None):
+        """Run the steps; keep the FP64 state at the start of every segment.
+        Returns device views (r[n,3], v[n,3]) of the final state."""
+        n = self.fwd.info.n_bodies
+        self.fwd.set_state(r0, v0, gm, stream=stream)
+        self.checkpoints = []
+        k = 0
+        while k < self.steps:
+            self.checkpoints.append((self.fwd.r[:n].clone(), self.fwd.v[:n].clone()))
+            c = min(self.every, self.steps - k)
+            self.fwd.step(c, stream=stream)
+            k += c
+        self.final = (self.fwd.r[:n].clone(), self.fwd.v[:n].clone())
+        return self.fwd.r[:n, :3], self.fwd.v[:n, :3]
+
+    def backward(self, g_r, g_v, stream=None):
+        """Gradients (dL/dr0 [n,3], dL/dv0 [n,3], dL/dGm [n]) from dL/dr_K, dL/dv_K."""
+        a = self.adj
+        n = a.info.n_bodies
+        a.gr.zero_()
+        a.gv.zero_()
+        a.ggm.zero_()
+        a.gr[:n, :3].copy_(g_r)
+        a.gv[:n, :3].copy_(g_v)
+        starts = list(range(0, self.steps, self.every))
+        for si in reversed(range(len(starts))):
+            end = starts[si + 1] if si + 1 < len(starts) else self.steps
+            state = self.checkpoints[si + 1] if si + 1 < len(starts) else self.final
+            a.set_state(*state)
+            a.prepare(stream)
+            for _ in range(end - starts[si]):
+                a.step(stream)
+        self.reversed_state = (a.r[:n, :3].clone(), a.v[:n, :3].clone())
+        return a.gr[:n, :3].clone(), a.gv[:n, :3].clone(), a.ggm[:n].clone()
+
+
+class _RolloutFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, r0, v0, m, G, ro):
+        gm = (float(G) * m).detach()
+        rK, vK = ro.forward(r0.detach(), v0.detach(), gm)
+        ctx.ro = ro
+        ctx.G = float(G)
+        return rK.clone(), vK.clone()
+
+    @staticmethod
+    def backward(ctx, g_rK, g_vK):
+        ro = ctx.ro
+        if g_rK is None:
+            g_rK = torch.zeros_like(ro.final[0][:, :3])
+        if g_vK is None:
+            g_vK = torch.zeros_like(ro.final[1][:, :3])
+        gr, gv, ggm = ro.backward(g_rK.to(torch.float64), g_vK.to(torch.float64))
+        ro.adj.raise_on_device_error()
+        return gr, gv, ctx.G * ggm, None, None
+
+
+def rollout(r0, v0, m, G, T, steps, every=32, ro=None):
+    """Differentiable K-step rollout of one universe (or a packed batch when ``ro`` is
+    given).  r0, v0: [n,3] float64 CUDA tensors; m: [n] masses (scaled); G: scaled
+    gravitational constant.  Returns (r_K, v_K)."""
+    if ro is None:
+        ro = Rollout([r0.shape[0]], T, steps, every, device=r0.device.index)
+    return _RolloutFn.apply(r0, v0, m, G, ro)
+
+
+def torch_reference_rollout(r0, v0, m, G, T, steps):
+    """Plain PyTorch FP64 integrator (autograd reference): the same law and update."""
+    n = r0.shape[0]
+    eye = torch.eye(n, dtype=r0.dtype, device=r0.device)
+    r, v = r0, v0
+    for _ in range(steps):
+        d = r[None, :, :] - r[:, None, :]          # d[i, j] = r_j - r_i
+        r2 = (d * d).sum(-1) + eye
+        inv3 = r2.pow(-1.5) * (1.0 - eye)
+        a = G * (d * (m[None, :, None] * inv3[:, :, None])).sum(1)
+        v = v + T * a
+        r = r + T * v
+    return r, v

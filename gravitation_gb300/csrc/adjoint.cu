@@ -1,0 +1,343 @@
+// adjoint.cu -- discrete adjoint (reverse-mode gradient) of the step, for gradients of
+// a loss on the final state with respect to initial positions, velocities and masses.
+//
+// Forward step k (symplectic Euler, _base_.py:58-62):
+//     a_k = A(r_k),  v_{k+1} = v_k + T a_k,  r_{k+1} = r_k + T v_{k+1}
+//     A_i(r) = sum_{j!=i} Gm_j f(r_j - r_i),  f(d) = d/|d|^3
+// Backward step k, given gr = dL/dr_{k+1}, gv = dL/dv_{k+1}:
+//     u   = gv + T gr                         (dL/dv_{k+1} through both uses)
+//     gr <- gr + T h_k,   h_k = J_A(r_k)^T u
+//     gv <- u
+//     gGm_j <- gGm_j + T sum_{i!=j} u_i . f(r_j - r_i)  = gGm_j - T g_j
+// with, per ordered pair (k, j), d = r_j - r_k and Jf(d) = I/|d|^3 - 3 d d^T/|d|^5,
+//     h_k = sum_j Jf(d) (Gm_k u_j - Gm_j u_k)
+//         = Gm_k sum_j u_j/|d|^3 - u_k sum_j Gm_j/|d|^3 - 3 sum_j (Gm_k d.u_j - Gm_j d.u_k) d/|d|^5
+//     g_k = sum_j u_j . d / |d|^3
+// Zero separations (the self pair, coincident bodies) are excluded exactly (the
+// reciprocal distance is selected to 0), so no large self terms enter the sums.
+//
+// The state needed by step k is not stored: the backward sweep reverses the forward
+// update in FP64,  r_k = r_{k+1} - T v_{k+1},  v_k = v_{k+1} - T a_k,  and recomputes
+// a_k = A(r_k) (stage 1) inside the same pair kernel as h and g.  The caller resets the
+// reversed state to the stored FP64 checkpoint at the start of every checkpoint
+// segment, so rounding in the reversal never accumulates over more than one segment.
+//
+// Pair kernel: persistent stage-1 work list (pairs_skeleton.cuh), j-tiles of FP32
+// positions (x, y, z, Gm) and FP32 u, FP32 tile partials folded into FP64; 7 outputs
+// per body (a, h, g) in the partial slots.  Adjoint stage 2 (one thread per padded row)
+// sums the slots and applies the updates above in FP64, then prepares the FP32
+// positions r_{k-1} and u for the next backward step.
+#include "pairs_skeleton.cuh"
+
+namespace grav {
+
+int record_error(int code, const char* msg);
+
+template <int B_, int T_, int J_>
+struct VjpOp {
+	static constexpr int B = B_, T = T_, J = J_, NP = 2, NC = 7;
+	using Elem = float4;
+	const float4* pos;
+	const float4* upos;
+	float xi[B], yi[B], zi[B], gmi[B], uxi[B], uyi[B], uzi[B];
+	float fa[3][B], fp[3][B], fq[3][B], fs[B], fg[B];
+	double da[3][B], dh[3][B], dg[B];
+
+	__device__ const Elem* jsrc(int a) const { return a == 0 ? pos : upos; }
+
+	__device__ void begin(int64_t ibase, int tid)
+	{
+#pragma unroll
+		for (int k = 0; k < B; ++k) {
+			const float4 p = pos[ibase + tid + k * T];
+			const float4 q = upos[ibase + tid + k * T];
+			xi[k] = p.x;
+			yi[k] = p.y;
+			zi[k] = p.z;
+			gmi[k] = p.w;
+			uxi[k] = q.x;
+			uyi[k] = q.y;
+			uzi[k] = q.z;
+#pragma unroll
+			for (int c = 0; c < 3; ++c) {
+				fa[c][k] = fp[c][k] = fq[c][k] = 0.f;
+				da[c][k] = dh[c][k] = 0.0;
+			}
+			fs[k] = fg[k] = 0.f;
+			dg[k] = 0.0;
+		}
+	}
+
+	__device__ void tile(const Elem* const* s)
+	{
+		const float4* sp = s[0];
+		const float4* su = s[1];
+#pragma unroll 2
+		for (int j = 0; j < J; ++j) {
+			const float4 pj = sp[j];
+			const float4 uj = su[j];
+#pragma unroll
+			for (int k = 0; k < B; ++k) {
+				const float dx = pj.x - xi[k], dy = pj.y - yi[k], dz = pj.z - zi[k];
+				const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+				const float inv = (r2 > 0.f) ? rsqrt_sfu(r2) : 0.f;
+				const float inv2 = inv * inv;
+				const float inv3 = inv2 * inv;
+				const float m3inv5 = inv3 * (-3.f * inv2);
+				const float c = pj.w * inv3;  // Gm_j / r^3
+				fa[0][k] = fmaf(c, dx, fa[0][k]);
+				fa[1][k] = fmaf(c, dy, fa[1][k]);
+				fa[2][k] = fmaf(c, dz, fa[2][k]);
+				fs[k] += c;
+				fp[0][k] = fmaf(uj.x, inv3, fp[0][k]);
+				fp[1][k] = fmaf(uj.y, inv3, fp[1][k]);
+				fp[2][k] = fmaf(uj.z, inv3, fp[2][k]);
+				const float duj = fmaf(dz, uj.z, fmaf(dy, uj.y, dx * uj.x));
+				const float duk = fmaf(dz, uzi[k], fmaf(dy, uyi[k], dx * uxi[k]));
+				const float dw = fmaf(gmi[k], duj, -pj.w * duk);
+				const float t = dw * m3inv5;
+				fq[0][k] = fmaf(t, dx, fq[0][k]);
+				fq[1][k] = fmaf(t, dy, fq[1][k]);
+				fq[2][k] = fmaf(t, dz, fq[2][k]);
+				fg[k] = fmaf(duj, inv3, fg[k]);
+			}
+		}
+		// fold the tile's FP32 partials into FP64
+#pragma unroll
+		for (int k = 0; k < B; ++k) {
+#pragma unroll
+			for (int c3 = 0; c3 < 3; ++c3) {
+				da[c3][k] += static_cast<double>(fa[c3][k]);
+				fa[c3][k] = 0.f;
+			}
+			const float ui[3] = {uxi[k], uyi[k], uzi[k]};
+#pragma unroll
+			for (int c3 = 0; c3 < 3; ++c3) {
+				// h = Gm_k P - u_k S + Q   (the -3 is folded into t)
+				dh[c3][k] += static_cast<double>(gmi[k]) * fp[c3][k] -
+					static_cast<double>(ui[c3]) * fs[k] + static_cast<double>(fq[c3][k]);
+				fp[c3][k] = fq[c3][k] = 0.f;
+			}
+			dg[k] += static_cast<double>(fg[k]);
+			fs[k] = fg[k] = 0.f;
+		}
+	}
+
+	__device__ void store(double* out, int tid)
+	{
+		constexpr int IT = B * T;
+#pragma unroll
+		for (int k = 0; k < B; ++k) {
+			const int i = tid + k * T;
+			out[0 * IT + i] = da[0][k];
+			out[1 * IT + i] = da[1][k];
+			out[2 * IT + i] = da[2][k];
+			out[3 * IT + i] = dh[0][k];
+			out[4 * IT + i] = dh[1][k];
+			out[5 * IT + i] = dh[2][k];
+			out[6 * IT + i] = dg[k];
+		}
+	}
+};
+
+template <int B, int T, int J>
+__global__ void __launch_bounds__(T) vjp_kernel(const grav_batch b, const float4* upos)
+{
+	VjpOp<B, T, J> op;
+	op.pos = static_cast<const float4*>(b.pos);
+	op.upos = upos;
+	run_pairs(b, op);
+}
+
+struct __align__(32) arow4 {
+	double x, y, z, w;
+};
+
+// flags of the adjoint stage 2
+#define ADJ_STEP 1     // apply one backward step from the pair kernel's sums
+#define ADJ_PREPARE 2  // write FP32 r_{k-1} = r - T v and u = gv + T gr for the pair kernel
+
+__global__ void __launch_bounds__(256) adjoint_stage2_kernel(const grav_batch b, double* gr,
+	double* gv, double* ggm, float4* upos, const int flags)
+{
+	const int64_t g = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (g >= b.n_pad_total) return;
+	const int IT = b.tile.bpt * b.tile.threads;
+	const int64_t seg = g / IT;
+	const int li = static_cast<int>(g - seg * IT);
+	const grav_seg_desc S = b.seg[seg];
+	const grav_univ_desc U = b.univ[S.u];
+	const int il = S.il0 + li;
+	float4* pos = static_cast<float4*>(b.pos);
+	if (il >= U.n) {
+		pos[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+		upos[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+		return;
+	}
+	const int64_t row = U.body_off + il;
+	const double T = U.T;
+	arow4* rr = reinterpret_cast<arow4*>(b.r);
+	arow4* vv = reinterpret_cast<arow4*>(b.v);
+	arow4* grr = reinterpret_cast<arow4*>(gr);
+	arow4* gvv = reinterpret_cast<arow4*>(gv);
+	arow4 r = rr[row], v = vv[row], a_gr = grr[row], a_gv = gvv[row];
+
+	if (flags & ADJ_STEP) {
+		double s[7] = {0, 0, 0, 0, 0, 0, 0};
+		for (int k = 0; k < S.nslots; ++k) {
+			const double* p = b.part + static_cast<int64_t>(S.slot_base + k) * 7 * IT + li;
+#pragma unroll
+			for (int c = 0; c < 7; ++c) s[c] += p[c * IT];
+		}
+		// reverse the forward update: r_k = r_{k+1} - T v_{k+1}; v_k = v_{k+1} - T a_k
+		r.x = __dsub_rn(r.x, __dmul_rn(v.x, T));
+		r.y = __dsub_rn(r.y, __dmul_rn(v.y, T));
+		r.z = __dsub_rn(r.z, __dmul_rn(v.z, T));
+		v.x = __dsub_rn(v.x, __dmul_rn(s[0], T));
+		v.y = __dsub_rn(v.y, __dmul_rn(s[1], T));
+		v.z = __dsub_rn(v.z, __dmul_rn(s[2], T));
+		// gradients
+		const double ux = a_gv.x + T * a_gr.x, uy = a_gv.y + T * a_gr.y, uz = a_gv.z + T * a_gr.z;
+		a_gr.x += T * s[3];
+		a_gr.y += T * s[4];
+		a_gr.z += T * s[5];
+		a_gv.x = ux;
+		a_gv.y = uy;
+		a_gv.z = uz;
+		ggm[row] -= T * s[6];
+		rr[row] = r;
+		vv[row] = v;
+		grr[row] = a_gr;
+		gvv[row] = a_gv;
+	}
+	if (flags & ADJ_PREPARE) {
+		// position of the next backward step and the u it contracts with
+		const double px = __dsub_rn(r.x, __dmul_rn(v.x, T));
+		const double py = __dsub_rn(r.y, __dmul_rn(v.y, T));
+		const double pz = __dsub_rn(r.z, __dmul_rn(v.z, T));
+		pos[g] = make_float4(__double2float_rn(px), __double2float_rn(py), __double2float_rn(pz),
+			__double2float_rn(r.w));
+		upos[g] = make_float4(__double2float_rn(a_gv.x + T * a_gr.x),
+			__double2float_rn(a_gv.y + T * a_gr.y), __double2float_rn(a_gv.z + T * a_gr.z), 0.f);
+	}
+}
+
+struct VjpKernel {
+	int bpt, threads, jtile;
+	const void* fn;
+	int smem;
+};
+
+#define GRAV_VJP_ENTRY(B, T, J) \
+	{B, T, J, reinterpret_cast<const void*>(&vjp_kernel<B, T, J>), \
+		pairs_smem_bytes<VjpOp<B, T, J>>()}
+
+static const VjpKernel k_vjp[] = {
+	GRAV_VJP_ENTRY(1, 128, 128),
+	GRAV_VJP_ENTRY(2, 128, 128),
+	GRAV_VJP_ENTRY(2, 256, 128),
+	GRAV_VJP_ENTRY(4, 128, 128),
+};
+
+int vjp_table(const VjpKernel** out)
+{
+	*out = k_vjp;
+	return static_cast<int>(sizeof(k_vjp) / sizeof(k_vjp[0]));
+}
+
+}  // namespace grav
+
+namespace {
+
+int check_adj(const grav_adjoint* a)
+{
+	using grav::record_error;
+	if (!a || !a->b) return record_error(GRAV_E_ARG, "NULL adjoint or batch");
+	const grav_batch* b = a->b;
+	if (b->mode != GRAV_MODE_FP32)
+		return record_error(GRAV_E_ARG, "the adjoint runs on an FP32-mode batch (float4 positions)");
+	if (!b->univ || !b->seg || !b->pos || !b->r || !b->v || !b->err)
+		return record_error(GRAV_E_ARG, "NULL device pointer in grav_batch");
+	if (!a->gr || !a->gv || !a->ggm || !a->upos || !a->part7)
+		return record_error(GRAV_E_ARG, "NULL device pointer in grav_adjoint");
+	const int64_t itile = static_cast<int64_t>(b->tile.bpt) * b->tile.threads;
+	if (b->n_pad_total != static_cast<int64_t>(b->n_seg) * itile)
+		return record_error(GRAV_E_ARG, "n_pad_total != n_seg * itile");
+	return GRAV_OK;
+}
+
+}  // namespace
+
+extern "C" int grav_adjoint_tile_supported(const grav_tile* t)
+{
+	if (!t) return 0;
+	const grav::VjpKernel* tab = nullptr;
+	const int n = grav::vjp_table(&tab);
+	for (int i = 0; i < n; ++i)
+		if (tab[i].bpt == t->bpt && tab[i].threads == t->threads && tab[i].jtile == t->jtile) return 1;
+	return 0;
+}
+
+extern "C" int grav_adjoint_occupancy(const grav_tile* t, int32_t* ctas_per_sm)
+{
+	if (!t || !ctas_per_sm) return grav::record_error(GRAV_E_ARG, "NULL argument");
+	const grav::VjpKernel* tab = nullptr;
+	const int n = grav::vjp_table(&tab);
+	for (int i = 0; i < n; ++i)
+		if (tab[i].bpt == t->bpt && tab[i].threads == t->threads && tab[i].jtile == t->jtile) {
+			int blocks = 0;
+			cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, tab[i].fn,
+				tab[i].threads, tab[i].smem);
+			if (e != cudaSuccess) return grav::record_error(GRAV_E_CUDA, cudaGetErrorString(e));
+			*ctas_per_sm = blocks;
+			return GRAV_OK;
+		}
+	return grav::record_error(GRAV_E_TILE, "tile shape has no adjoint kernel");
+}
+
+extern "C" int grav_adjoint_prepare(const grav_adjoint* a, void* stream)
+{
+	int rc = check_adj(a);
+	if (rc) return rc;
+	const grav_batch& b = *a->b;
+	if (b.n_pad_total == 0) return GRAV_OK;
+	grav_batch copy = b;
+	copy.part = a->part7;
+	const unsigned blocks = static_cast<unsigned>((b.n_pad_total + 255) / 256);
+	grav::adjoint_stage2_kernel<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+		copy, a->gr, a->gv, a->ggm, static_cast<float4*>(a->upos), ADJ_PREPARE);
+	cudaError_t e = cudaGetLastError();
+	return e == cudaSuccess ? GRAV_OK : grav::record_error(GRAV_E_CUDA, cudaGetErrorString(e));
+}
+
+extern "C" int grav_adjoint_step(const grav_adjoint* a, void* stream)
+{
+	int rc = check_adj(a);
+	if (rc) return rc;
+	const grav_batch& b = *a->b;
+	if (b.n_pad_total == 0) return GRAV_OK;
+	cudaStream_t st = static_cast<cudaStream_t>(stream);
+	grav_batch copy = b;
+	copy.part = a->part7;
+	if (b.n_units > 0) {
+		if (b.tile.grid <= 0 || b.tile.grid > b.n_units)
+			return grav::record_error(GRAV_E_ARG, "tile.grid must be in [1, n_units]");
+		const grav::VjpKernel* tab = nullptr;
+		const int n = grav::vjp_table(&tab);
+		const grav::VjpKernel* k = nullptr;
+		for (int i = 0; i < n; ++i)
+			if (tab[i].bpt == b.tile.bpt && tab[i].threads == b.tile.threads &&
+				tab[i].jtile == b.tile.jtile)
+				k = &tab[i];
+		if (!k) return grav::record_error(GRAV_E_TILE, "tile shape has no adjoint kernel");
+		const float4* up = static_cast<const float4*>(a->upos);
+		void* args[] = {&copy, &up};
+		cudaError_t e = cudaLaunchKernel(k->fn, dim3(b.tile.grid), dim3(k->threads), args, k->smem, st);
+		if (e != cudaSuccess) return grav::record_error(GRAV_E_CUDA, cudaGetErrorString(e));
+	}
+	const unsigned blocks = static_cast<unsigned>((b.n_pad_total + 255) / 256);
+	grav::adjoint_stage2_kernel<<<blocks, 256, 0, st>>>(copy, a->gr, a->gv, a->ggm,
+		static_cast<float4*>(a->upos), ADJ_STEP | ADJ_PREPARE);
+	cudaError_t e = cudaGetLastError();
+	return e == cudaSuccess ? GRAV_OK : grav::record_error(GRAV_E_CUDA, cudaGetErrorString(e));
+}

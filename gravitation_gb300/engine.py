@@ -243,11 +243,53 @@ class Engine:
         for _ in range(int(steps)):
             check(self.lib.grav_step(self._bref, flags, h))
 
+    def capture_graph(self, steps=1):
+        """CUDA graph of `steps` full steps (the steady-state step: stage 1 + stage 2,
+        2 launches per step); returns a torch.cuda.CUDAGraph whose replay() runs them.
+        The launches are recorded on a side stream that torch puts into capture mode."""
+        side = torch.cuda.Stream(device=self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=side):
+            self.step(steps, stream=side)
+        torch.cuda.current_stream(self.device).wait_stream(side)
+        return g
+
     def forces(self, stream=None):
         """Stage 1 only; returns the accelerations (float64 [n_bodies, 3], device)."""
         self.stage1(stream)
         self.stage2(_lib.GRAV_S2_WRITE_A, stream)
         return self.a[:self.info.n_bodies, :3]
+
+    # ---- diagnostics ----------------------------------------------------------------
+    def _fp64_view(self):
+        """An FP64-mode batch sharing r, v and the plan, with its own padded double4
+        positions and partial-sum scratch (so a diagnostic never clobbers stage 1)."""
+        if getattr(self, '_b64', None) is None:
+            info = self.info
+            nbytes = int(self.lib.grav_pos_bytes(_lib.GRAV_MODE_FP64, info.n_pad_total))
+            self._pos64 = torch.zeros(max(nbytes // 8, 4), dtype=torch.float64, device=self.device)
+            self._part64 = torch.zeros_like(self.part)
+            self._out64 = torch.zeros(max(info.n_univ, 1) * 8, dtype=torch.float64,
+                                      device=self.device)
+            b = _lib.Batch()
+            ctypes.pointer(b)[0] = self.batch
+            b.mode = _lib.GRAV_MODE_FP64
+            b.pos = self._pos64.data_ptr()
+            b.part = self._part64.data_ptr()
+            self._b64 = b
+        return self._b64
+
+    def energy(self, G, stream=None):
+        """FP64 (kinetic, potential, momentum[3]) per universe as a numpy array
+        [n_univ, 5]; G is the (scaled) gravitational constant of the universes."""
+        b = self._fp64_view()
+        h = self._h(stream)
+        check(self.lib.grav_prepare(ctypes.byref(b), h))
+        check(self.lib.grav_energy(ctypes.byref(b), ctypes.c_void_p(self._out64.data_ptr()), h))
+        out = self._out64.view(-1, 8)[:self.info.n_univ, :5].cpu().numpy() / float(G)
+        self.raise_on_device_error()
+        return out
 
     # ---- errors ---------------------------------------------------------------------
     def device_error(self):

@@ -1,0 +1,158 @@
+"""Measured workloads beyond the single-universe step (used by bench.py).
+
+  run_batched   many universes of log-uniform size (64..16384) in one persistent launch
+                per stage, the steady-state step replayed from a CUDA graph, tile shape
+                from the autotuner -- against looping the single-universe step over the
+                universes (one Engine per universe, each with its own tuned tile)
+"""
+
+import statistics
+import time
+
+import numpy as np
+import torch
+
+from .engine import Engine
+from .scenarios import G_DEFAULT, T_DEFAULT, batch_universes
+
+
+def run_adjoint(n=4096, steps=1000, every=32, seed=3, reps=3, tuner=None, device=None):
+    """Forward rollout vs forward + adjoint (gradients of the mean squared distance to a
+    target made by the same run with masses scaled by a seeded factor in [0.99, 1.01]).
+    Returns timings and the steps/s of forward+adjoint."""
+    from .adjoint import Rollout
+    from .scenarios import mass_perturbation, uniform_cube
+    r, v, m = uniform_cube(n, seed=seed)
+    dev = torch.device('cuda', torch.cuda.current_device() if device is None else device)
+    gm = torch.tensor(G_DEFAULT * m, device=dev)
+    gm_t = torch.tensor(G_DEFAULT * m * mass_perturbation(n, seed), device=dev)
+    r0 = torch.tensor(r, device=dev)
+    v0 = torch.tensor(v, device=dev)
+    ro = Rollout([n], T_DEFAULT, steps, every, device=dev.index, tuner=tuner)
+    rt, _ = ro.forward(r0, v0, gm_t)
+    rt = rt.clone()
+    stream = torch.cuda.current_stream(dev)
+    fwd_ms, tot_ms = [], []
+    for _ in range(reps):
+        e0, e1 = _events(1)[0]
+        e2 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        rK, _ = ro.forward(r0, v0, gm)
+        e1.record(stream)
+        g_r = (2.0 / n) * (rK - rt)
+        ro.backward(g_r, torch.zeros_like(g_r))
+        e2.record(stream)
+        e2.synchronize()
+        fwd_ms.append(e0.elapsed_time(e1))
+        tot_ms.append(e0.elapsed_time(e2))
+    ro.adj.raise_on_device_error()
+    ro.fwd.raise_on_device_error()
+    f, t = min(fwd_ms), min(tot_ms)
+    return {
+        'workload': 'N=%d uniform cube seed %d, %d steps, checkpoint every %d, loss = mean '
+                    '|r_K - r_target|^2 (target: masses x U[0.99,1.01])' % (n, seed, steps, every),
+        'forward_ms': f, 'forward_adjoint_ms': t, 'ratio_fwd_plus_adjoint_over_fwd': t / f,
+        'fwd_adjoint_steps_per_s': steps / (t * 1e-3),
+        'launches_per_step': {'forward': 2, 'adjoint': 2},
+    }
+
+
+def _events(n):
+    return [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            for _ in range(n)]
+
+
+def run_batched(steps=100, warmup=3, mode='fp32', n_univ=256, seed=1, loop_steps=10,
+                tuner=None, device=None):
+    """Batched step vs the per-universe loop.  Returns a dict of measurements."""
+    sizes, states = batch_universes(n_univ, seed)
+    sizes = [int(s) for s in sizes]
+    r = np.concatenate([s[0] for s in states])
+    v = np.concatenate([s[1] for s in states])
+    gm = G_DEFAULT * np.concatenate([s[2] for s in states])
+    inter = float(sum(n * n for n in sizes))
+    dev = torch.device('cuda', torch.cuda.current_device() if device is None else device)
+    stream = torch.cuda.current_stream(dev)
+
+    eng = Engine(sizes, T_DEFAULT, mode=mode, tuner=tuner, device=dev.index)
+    eng.set_state(r, v, gm)
+    graph = eng.capture_graph(1)
+    for _ in range(warmup):
+        graph.replay()
+    torch.cuda.synchronize()
+    e0, e1 = _events(1)[0]
+    e0.record(stream)
+    for _ in range(steps):
+        graph.replay()
+    e1.record(stream)
+    e1.synchronize()
+    eng.raise_on_device_error()
+    batched_ms = e0.elapsed_time(e1) / steps
+
+    # the same batch, launched step by step without the graph
+    e0.record(stream)
+    eng.step(steps)
+    e1.record(stream)
+    e1.synchronize()
+    nograph_ms = e0.elapsed_time(e1) / steps
+
+    # per-universe loop of the single-universe step
+    engines = []
+    off = 0
+    for n in sizes:
+        e = Engine([n], T_DEFAULT, mode=mode, tuner=tuner, device=dev.index)
+        e.set_state(r[off:off + n], v[off:off + n], gm[off:off + n])
+        engines.append(e)
+        off += n
+    for _ in range(warmup):
+        for e in engines:
+            e.step(1)
+    torch.cuda.synchronize()
+    walls = []
+    e0.record(stream)
+    for _ in range(loop_steps):
+        t0 = time.perf_counter()
+        for e in engines:
+            e.step(1)
+        torch.cuda.synchronize()
+        walls.append(time.perf_counter() - t0)
+    e1.record(stream)
+    e1.synchronize()
+    loop_ms = 1e3 * statistics.mean(walls)
+    # the loop captured in one graph: its GPU-side cost without host launch overhead
+    side = torch.cuda.Stream(device=dev)
+    side.wait_stream(stream)
+    g2 = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g2, stream=side):
+        for e in engines:
+            e.step(1, stream=side)
+    stream.wait_stream(side)
+    g2.replay()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(loop_steps):
+        g2.replay()
+    e1.record(stream)
+    e1.synchronize()
+    loop_graph_ms = e0.elapsed_time(e1) / loop_steps
+    for e in engines:
+        e.raise_on_device_error()
+
+    return {
+        'workload': '%d universes, N log-uniform in [64,16384] (seed %d), uniform cube each, '
+                    '%s stage 1 + FP64 stage 2' % (n_univ, seed, mode),
+        'interactions_per_step': inter,
+        'bodies': int(sum(sizes)),
+        'batched_ms_per_step': batched_ms,
+        'batched_interactions_per_s': inter / (batched_ms * 1e-3),
+        'batched_no_graph_ms_per_step': nograph_ms,
+        'loop_ms_per_step': loop_ms,
+        'loop_graph_ms_per_step': loop_graph_ms,
+        'speedup_vs_loop': loop_ms / batched_ms,
+        'speedup_vs_graphed_loop': loop_graph_ms / batched_ms,
+        'tile': {'bpt': eng.tile.bpt, 'threads': eng.tile.threads, 'jtile': eng.tile.jtile,
+                 'grid': eng.info.grid},
+        'launches_per_step': 2,
+        'loop_launches_per_step': 2 * n_univ,
+    }

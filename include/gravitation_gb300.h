@@ -190,6 +190,56 @@ int grav_stage2(const grav_batch* b, int flags, void* stream);
  * Replaces universe_base.step's stage 1 and stage 2 calls (_base_.py:143-144). */
 int grav_step(const grav_batch* b, int flags, void* stream);
 
+/* ---- diagnostics -------------------------------------------------------------------- */
+
+/*
+ * Energy and momentum of every universe in FP64.  `b` is an FP64 view of the batch:
+ * mode GRAV_MODE_FP64, pos = padded double4 positions refreshed by grav_prepare on that
+ * view, part = scratch of grav_part_bytes() (overwritten).  out: n_univ x 8 doubles
+ * (device), per universe
+ *   [0] sum 1/2 Gm v^2   [1] -1/2 sum_i Gm_i sum_{j!=i} Gm_j / |r_j - r_i|
+ *   [2..4] sum Gm v      [5..7] 0
+ * (divide by G for kinetic energy, potential energy and momentum).  Reduction order is
+ * fixed, so results are reproducible.  No reference counterpart (an accuracy analysis
+ * is a wish in the reference, TODO.md:4).
+ */
+int grav_energy(const grav_batch* b, double* out, void* stream);
+
+/* ---- adjoint (reverse-mode gradients) -------------------------------------------------- */
+
+/* Buffers of the backward sweep.  `b` is an FP32-mode batch planned with an adjoint
+ * tile (grav_adjoint_tile_supported); b->r, b->v hold the state being reversed (start:
+ * the state after the last forward step of the segment), b->pos is scratch. */
+typedef struct grav_adjoint {
+	const grav_batch* b;
+	double* gr;    /* n_bodies x 4: dL/dr of the current state (in/out) */
+	double* gv;    /* n_bodies x 4: dL/dv of the current state (in/out) */
+	double* ggm;   /* n_bodies: dL/d(G m), accumulated (in/out) */
+	void* upos;    /* float4 [n_pad_total]: scratch, FP32 u = gv + T gr of the next step */
+	double* part7; /* n_slots x 7 x itile doubles: scratch */
+} grav_adjoint;
+
+/* 1 if `tile` has a compiled adjoint pair kernel. */
+int grav_adjoint_tile_supported(const grav_tile* tile);
+
+/* Resident CTAs per SM of the adjoint pair kernel for `tile` on the current device. */
+int grav_adjoint_occupancy(const grav_tile* tile, int32_t* ctas_per_sm);
+
+/* Start of a backward segment: from b->r, b->v (state k+1) and gr, gv, write the FP32
+ * positions r_k = r_{k+1} - T v_{k+1} and u = gv + T gr used by the next step. */
+int grav_adjoint_prepare(const grav_adjoint* a, void* stream);
+
+/*
+ * One backward step through stage 2 and stage 1 (the adjoint kernel pair): a pair
+ * kernel recomputes a_k = A(r_k) (stage 1) and forms h = J_A(r_k)^T u and
+ * g_j = sum_i u_i.(r_i - r_j)/|r_i - r_j|^3; the adjoint stage 2 reverses the state
+ * (r_k = r_{k+1} - T v_{k+1}, v_k = v_{k+1} - T a_k, FP64), updates
+ * gr += T h, gv = u, ggm -= T g, and prepares the next step.
+ * Transposes universe_base.step_stage1/step_stage2 (_base_.py:147-156); no
+ * counterpart in the reference (it has no gradients).
+ */
+int grav_adjoint_step(const grav_adjoint* a, void* stream);
+
 /* ---- allocation-free variant ------------------------------------------------------- */
 
 /* Largest universe grav_forces_noalloc accepts. */

@@ -1,0 +1,126 @@
+"""GPU tests of the adjoint (csrc/adjoint.cu, gravitation_gb300/adjoint.py).
+
+Gradients of L = mean_i |r_K,i - t_i|^2 with respect to r0, v0 and m, checked against
+  - the FP64 oracle's vector-Jacobian product for a single step,
+  - autograd through a plain PyTorch FP64 integrator (same law, same update),
+  - FP64 central finite differences (eps 1e-6) on 16 seeded coordinates.
+The systems used here are compact and slow (velocities ~ the virial speed), so that
+gravity, not free streaming, shapes the final state and finite differences in FP64
+resolve the mass gradients.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from gravitation_gb300.adjoint import Rollout, rollout, torch_reference_rollout
+from gravitation_gb300.scenarios import G_DEFAULT, mass_perturbation, uniform_cube
+
+pytestmark = pytest.mark.gpu
+
+T = 1.0e3
+
+
+def compact(n, seed):
+    # half-width 100: over tens of steps gravity moves bodies by ~0.1, so a 1e-6 change
+    # of a mass moves final positions by ~1e-9, far above their FP64 resolution (~1e-14)
+    r, v, m = uniform_cube(n, seed=seed, half=100.0, v_sigma=1e-4)
+    return r, v, m
+
+
+def relerr(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def test_single_step_against_oracle_vjp(gpu):
+    n = 700
+    r, v, m = compact(n, 3)
+    rng = np.random.default_rng(1)
+    c = rng.normal(size=(n, 3))
+    ro = Rollout([n], T, 1, every=1)
+    dev = torch.device('cuda')
+    rK, vK = ro.forward(torch.tensor(r, device=dev), torch.tensor(v, device=dev),
+                        torch.tensor(G_DEFAULT * m, device=dev))
+    # L = sum c . r_1  ->  gr_1 = c, gv_1 = 0, u = T c
+    gr, gv, ggm = ro.backward(torch.tensor(c, device=dev), torch.zeros((n, 3), device=dev,
+                                                                        dtype=torch.float64))
+    u = T * c
+    h, g = oracle.vjp_fp64(r, m, G_DEFAULT, u)
+    assert relerr(gr.cpu().numpy(), c + T * h) < 1e-6
+    assert relerr(gv.cpu().numpy(), u) < 1e-15
+    # dL/dGm = -T g  (g_k = sum_j u_j . (r_j - r_k)/|r_j - r_k|^3)
+    assert relerr(ggm.cpu().numpy(), -T * g) < 1e-5
+    # the reversed state is the initial state
+    r_rev, v_rev = ro.reversed_state
+    assert np.max(np.abs(r_rev.cpu().numpy() - r)) <= 1e-12 * np.max(np.abs(r))
+    assert np.max(np.abs(v_rev.cpu().numpy() - v)) <= 1e-15 + 1e-9 * np.max(np.abs(v))
+
+
+@pytest.mark.parametrize('every', [1, 8, 40])
+def test_rollout_against_torch_autograd(gpu, every):
+    n, steps = 192, 40
+    r, v, m = compact(n, 5)
+    tgt = r + np.random.default_rng(2).normal(scale=1.0, size=r.shape)
+    dev = torch.device('cuda')
+    G = G_DEFAULT
+
+    def grads(fn):
+        r0 = torch.tensor(r, device=dev, requires_grad=True)
+        v0 = torch.tensor(v, device=dev, requires_grad=True)
+        mm = torch.tensor(m, device=dev, requires_grad=True)
+        rK, vK = fn(r0, v0, mm)
+        loss = ((rK - torch.tensor(tgt, device=dev)) ** 2).sum(1).mean()
+        loss.backward()
+        return [x.grad.cpu().numpy() for x in (r0, v0, mm)], float(loss)
+
+    ours, l1 = grads(lambda a, b, c: rollout(a, b, c, G, T, steps, every=every))
+    ref, l2 = grads(lambda a, b, c: torch_reference_rollout(a, b, c, G, T, steps))
+    assert abs(l1 - l2) <= 1e-6 * abs(l2)
+    for name, x, y in zip(('r0', 'v0', 'm'), ours, ref):
+        assert relerr(x, y) < 1e-5, (name, relerr(x, y))
+
+
+def test_rollout_against_finite_differences(gpu):
+    n, steps = 128, 30
+    r, v, m = compact(n, 7)
+    f = mass_perturbation(n, 7)
+    rt, _ = oracle.rollout_fp64(r, v, m * f, G_DEFAULT, T, steps)   # target run
+    dev = torch.device('cuda')
+    r0 = torch.tensor(r, device=dev, requires_grad=True)
+    v0 = torch.tensor(v, device=dev, requires_grad=True)
+    mm = torch.tensor(m, device=dev, requires_grad=True)
+    rK, _ = rollout(r0, v0, mm, G_DEFAULT, T, steps, every=8)
+    loss = ((rK - torch.tensor(rt, device=dev)) ** 2).sum(1).mean()
+    loss.backward()
+
+    def L(rr, vv, mv):
+        rk, _ = oracle.rollout_fp64(rr, vv, mv, G_DEFAULT, T, steps)
+        return float(((rk - rt) ** 2).sum(1).mean())
+
+    rng = np.random.default_rng(16)
+    eps = 1e-6
+    checks = []
+    for _ in range(16):
+        which = rng.integers(3)
+        i = int(rng.integers(n))
+        c = int(rng.integers(3))
+        rp, rm_, vp, vm, mp, mmn = r.copy(), r.copy(), v.copy(), v.copy(), m.copy(), m.copy()
+        if which == 0:
+            rp[i, c] += eps
+            rm_[i, c] -= eps
+            g = r0.grad[i, c].item()
+        elif which == 1:
+            vp[i, c] += eps
+            vm[i, c] -= eps
+            g = v0.grad[i, c].item()
+        else:
+            mp[i] += eps
+            mmn[i] -= eps
+            g = mm.grad[i].item()
+        fd = (L(rp, vp, mp) - L(rm_, vm, mmn)) / (2 * eps)
+        checks.append((which, g, fd))
+    for which, g, fd in checks:
+        assert abs(g - fd) <= 1e-4 * abs(fd) + 1e-12, (which, g, fd)

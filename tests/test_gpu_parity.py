@@ -231,6 +231,42 @@ def test_batched_matches_single(gpu):
         eng.raise_on_device_error()
 
 
+def test_energy_momentum_fp64(gpu):
+    """Energy and momentum of every universe of a batch against the FP64 oracle."""
+    sizes = [2, 300, 1500, 77]
+    rs, vs, ms = zip(*[uniform_cube(n, seed=70 + i) for i, n in enumerate(sizes)])
+    for mode in ('fp32', 'fp64'):
+        eng = Engine(sizes, 1e3, mode=mode)
+        eng.set_state(np.concatenate(rs), np.concatenate(vs), G_DEFAULT * np.concatenate(ms))
+        out = eng.energy(G_DEFAULT)
+        for u in range(len(sizes)):
+            k, p, mom = oracle.energy_fp64(rs[u], vs[u], ms[u], G_DEFAULT)
+            assert abs(out[u, 0] - k) <= 1e-12 * abs(k)
+            assert abs(out[u, 1] - p) <= 1e-12 * abs(p)
+            assert np.allclose(out[u, 2:5], mom, rtol=1e-12, atol=1e-12 * np.abs(ms[u]).sum())
+        # a step in between and the diagnostic does not disturb the state
+        eng.step(2)
+        out2 = eng.energy(G_DEFAULT)
+        assert np.all(np.isfinite(out2))
+
+
+def test_graph_replay_matches_launches(gpu):
+    """The CUDA-graph step replays exactly what the launched steps compute."""
+    sizes = [300, 64, 2000]
+    rs, vs, ms = zip(*[uniform_cube(n, seed=90 + i) for i, n in enumerate(sizes)])
+    r, v, gm = np.concatenate(rs), np.concatenate(vs), G_DEFAULT * np.concatenate(ms)
+    a = Engine(sizes, 1e3, mode='fp32')
+    a.set_state(r, v, gm)
+    a.step(4)
+    b = Engine(sizes, 1e3, mode='fp32', tile=a.tile)
+    b.set_state(r, v, gm)
+    g = b.capture_graph(2)
+    g.replay()
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(a.r, b.r) and torch.equal(a.v, b.v)
+
+
 def test_context_usable_after_many_launches(gpu):
     r, v, m = uniform_cube(2048, seed=1)
     eng = Engine([2048], 1e3, mode='fp32')
