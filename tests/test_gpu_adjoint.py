@@ -101,12 +101,16 @@ def test_rollout_against_finite_differences(gpu):
         return float(((rk - rt) ** 2).sum(1).mean())
 
     rng = np.random.default_rng(16)
-    eps = 1e-6
+    # central differences with eps = 1e-6 in units of each variable's scale: positions
+    # (~100) and masses (~50) take eps = 1e-6 directly; the velocities here are ~1e-4,
+    # where 1e-6 would be a 1 % change, so their step is 1e-6 * 1e-3
+    eps_of = {0: 1e-6, 1: 1e-9, 2: 1e-6}
     checks = []
     for _ in range(16):
-        which = rng.integers(3)
+        which = int(rng.integers(3))
         i = int(rng.integers(n))
         c = int(rng.integers(3))
+        eps = eps_of[which]
         rp, rm_, vp, vm, mp, mmn = r.copy(), r.copy(), v.copy(), v.copy(), m.copy(), m.copy()
         if which == 0:
             rp[i, c] += eps
