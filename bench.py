@@ -39,6 +39,8 @@ sys.path.insert(0, ROOT)
 METRIC = ('pair-interactions/s/GPU at N=65536 and fwd+adjoint steps/s at ≤1e-5 FP64 err')
 UNIT = 'interactions/s'
 FLOP_PER_INTERACTION = 20
+STAGE1_KERNEL = {'fp32': 'stage1_f32_kernel<FP32>', 'fp32c': 'stage1_f32_kernel<FP32C>',
+                 'fp64': 'stage1_f64_kernel', 'fp32u': 'stage1_sym_kernel'}
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -49,7 +51,7 @@ def parse():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', choices=('ours', 'reference'), default='ours')
     ap.add_argument('--n', type=int, default=65536)
-    ap.add_argument('--mode', default='fp32', choices=('fp32', 'fp32c', 'fp64'))
+    ap.add_argument('--mode', default='fp32u', choices=('fp32', 'fp32u', 'fp32c', 'fp64'))
     ap.add_argument('--cpu-seconds', type=float, default=4.0,
                     help='target seconds per CPU-baseline sample run (3 runs)')
     ap.add_argument('--no-cpu', action='store_true')
@@ -356,7 +358,7 @@ def run_ours(args):
         return 0
     s1_avg = statistics.mean(s1_ms)
     achieved = FLOP_PER_INTERACTION * n * n / (s1_avg * 1e-3)
-    traffic = read_profile_traffic()
+    traffic = read_profile_traffic(args.mode)
     line = {
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world,
         'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': max_ms,
@@ -373,7 +375,8 @@ def run_ours(args):
         'stage1_ms': s1_avg, 'step_ms_min': min(step_ms), 'wall_s_timed_region': t_wall,
         'roofline': {'bound': 'fp32', 'achieved': achieved / 1e12, 'peak': peak / 1e12,
                      'unit': 'TFLOP/s', 'frac': achieved / peak, 'traffic': traffic,
-                     'kernel': 'stage1_f32_kernel', 'flop_per_interaction': FLOP_PER_INTERACTION,
+                     'kernel': STAGE1_KERNEL.get(args.mode, args.mode),
+                     'flop_per_interaction': FLOP_PER_INTERACTION,
                      'peak_kind': 'measured live (grav_fp32_peak_probe FFMA kernel)',
                      'peak_formula_tflops_at_max_clock':
                          info.sm_count * 128 * 2 * (clk.get('sm_max_mhz') or 2070) * 1e6 / 1e12},
@@ -415,9 +418,9 @@ def run_e2e(args, r, v, m, local):
             'ms_per_step_min': 1e3 * min(times), 'path': 'gb1.universe.step(), host_sync=full'}
 
 
-def read_profile_traffic():
+def read_profile_traffic(mode):
     """DRAM bytes per stage-1 launch from the committed ncu summary, if present."""
-    p = os.path.join(ROOT, 'profiles', 'stage1_fp32_n65536.md')
+    p = os.path.join(ROOT, 'profiles', 'stage1_%s_n65536.md' % mode)
     try:
         with open(p) as f:
             for line in f:

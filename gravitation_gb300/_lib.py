@@ -24,11 +24,13 @@ GRAV_DEV_TIMEOUT = 1
 GRAV_MODE_FP32 = 0
 GRAV_MODE_FP32C = 1
 GRAV_MODE_FP64 = 2
+GRAV_MODE_FP32U = 3
 GRAV_S2_INTEGRATE = 1
 GRAV_S2_WRITE_A = 2
 GRAV_S2_PREPARE = 4
 
-MODES = {'fp32': GRAV_MODE_FP32, 'fp32c': GRAV_MODE_FP32C, 'fp64': GRAV_MODE_FP64}
+MODES = {'fp32': GRAV_MODE_FP32, 'fp32c': GRAV_MODE_FP32C, 'fp64': GRAV_MODE_FP64,
+         'fp32u': GRAV_MODE_FP32U}
 
 
 class GravError(RuntimeError):
@@ -99,6 +101,8 @@ _DECLS = {
     'grav_occupancy': (ctypes.c_int, [ctypes.c_int, _P(Tile), _P(ctypes.c_int32)]),
     'grav_plan': (ctypes.c_int, [ctypes.c_int32, _P(ctypes.c_int32), _P(ctypes.c_double),
                                  _P(Tile), _P(PlanInfo), _P(UnivDesc), _P(SegDesc)]),
+    'grav_plan_pairs': (ctypes.c_int, [ctypes.c_int32, _P(ctypes.c_int32), _P(ctypes.c_double),
+                                       _P(Tile), _P(PlanInfo), _P(UnivDesc), _P(SegDesc)]),
     'grav_pos_bytes': (ctypes.c_int64, [ctypes.c_int, ctypes.c_int64]),
     'grav_part_bytes': (ctypes.c_int64, [_P(PlanInfo)]),
     'grav_eps2': (ctypes.c_float, [ctypes.c_double]),

@@ -42,10 +42,17 @@ int cuda_fail(cudaError_t e, const char* what)
 	return fail(GRAV_E_CUDA, "%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
 }
 
+int stage1_table_for(int mode, const grav::Stage1Kernel** tab)
+{
+	if (mode == GRAV_MODE_FP64) return grav::stage1_table_f64(tab);
+	if (mode == GRAV_MODE_FP32U) return grav::stage1_table_sym(tab);
+	return grav::stage1_table_f32(tab);
+}
+
 const grav::Stage1Kernel* find_kernel(int mode, int bpt, int threads, int jtile)
 {
 	const grav::Stage1Kernel* tab = nullptr;
-	int n = (mode == GRAV_MODE_FP64) ? grav::stage1_table_f64(&tab) : grav::stage1_table_f32(&tab);
+	int n = stage1_table_for(mode, &tab);
 	for (int i = 0; i < n; ++i)
 		if (tab[i].mode == mode && tab[i].bpt == bpt && tab[i].threads == threads &&
 			tab[i].jtile == jtile)
@@ -55,7 +62,8 @@ const grav::Stage1Kernel* find_kernel(int mode, int bpt, int threads, int jtile)
 
 bool valid_mode(int mode)
 {
-	return mode == GRAV_MODE_FP32 || mode == GRAV_MODE_FP32C || mode == GRAV_MODE_FP64;
+	return mode == GRAV_MODE_FP32 || mode == GRAV_MODE_FP32C || mode == GRAV_MODE_FP64 ||
+		mode == GRAV_MODE_FP32U;
 }
 
 int check_batch(const grav_batch* b)
@@ -126,7 +134,7 @@ int grav_tile_list(int mode, grav_tile* out, int cap)
 {
 	if (!valid_mode(mode)) return fail(GRAV_E_ARG, "unknown precision mode %d", mode);
 	const grav::Stage1Kernel* tab = nullptr;
-	int n = (mode == GRAV_MODE_FP64) ? grav::stage1_table_f64(&tab) : grav::stage1_table_f32(&tab);
+	int n = stage1_table_for(mode, &tab);
 	int count = 0;
 	for (int i = 0; i < n; ++i) {
 		if (tab[i].mode != mode) continue;
@@ -228,6 +236,79 @@ int grav_plan(int32_t n_univ, const int32_t* n, const double* T, const grav_tile
 	info->n_slots = static_cast<int32_t>(slots);
 	info->itile = static_cast<int32_t>(itile);
 	info->pad_unit = static_cast<int32_t>(pad_unit);
+	info->grid = static_cast<int32_t>(grid);
+	if (univ_out && n_univ) std::memcpy(univ_out, univ.data(), sizeof(grav_univ_desc) * n_univ);
+	if (seg_out && n_seg) std::memcpy(seg_out, seg.data(), sizeof(grav_seg_desc) * n_seg);
+	return ok();
+}
+
+int grav_plan_pairs(int32_t n_univ, const int32_t* n, const double* T, const grav_tile* tile,
+	grav_plan_info* info, grav_univ_desc* univ_out, grav_seg_desc* seg_out)
+{
+	if (n_univ < 0) return fail(GRAV_E_ARG, "n_univ < 0");
+	if (n_univ > 0 && !n) return fail(GRAV_E_ARG, "n is NULL");
+	if (!tile || !info) return fail(GRAV_E_ARG, "tile or info is NULL");
+	if (tile->bpt <= 0 || tile->threads <= 0 || tile->jtile <= 0 || tile->grid <= 0)
+		return fail(GRAV_E_ARG, "tile sizes must be positive");
+	const auto pow2 = [](int x) { return x > 0 && (x & (x - 1)) == 0; };
+	if (!pow2(tile->bpt) || !pow2(tile->threads) || !pow2(tile->jtile) || tile->threads < 32)
+		return fail(GRAV_E_ARG, "tile sizes must be powers of two, threads >= 32");
+	const int64_t R = static_cast<int64_t>(tile->bpt) * tile->threads;  // rows per block
+	if (R % tile->jtile != 0) return fail(GRAV_E_ARG, "bpt*threads must be a multiple of jtile");
+	const int64_t tpb = R / tile->jtile;
+
+	std::vector<grav_univ_desc> univ(n_univ);
+	int64_t body = 0, pad = 0, units = 0;
+	for (int u = 0; u < n_univ; ++u) {
+		if (n[u] < 0) return fail(GRAV_E_ARG, "n[%d] = %d < 0", u, n[u]);
+		const int64_t nu = n[u];
+		const int64_t nb = (nu + R - 1) / R;
+		univ[u].body_off = body;
+		univ[u].pad_off = pad;
+		univ[u].n = static_cast<int32_t>(nu);
+		univ[u].n_jtiles = static_cast<int32_t>((nu + tile->jtile - 1) / tile->jtile);
+		univ[u].T = T ? T[u] : 0.0;
+		for (int64_t I = 0; I < nb; ++I) units += univ[u].n_jtiles - I * tpb;
+		body += nu;
+		pad += nb * R;
+	}
+	const int64_t n_seg64 = pad / R;
+	if (n_seg64 > INT32_MAX) return fail(GRAV_E_ARG, "too many segments");
+	const int32_t n_seg = static_cast<int32_t>(n_seg64);
+	const int64_t grid = units > 0 ? std::min<int64_t>(tile->grid, units) : 0;
+
+	std::vector<grav_seg_desc> seg(n_seg);
+	int64_t unit = 0, slots = 0;
+	int32_t s = 0;
+	for (int u = 0; u < n_univ; ++u) {
+		const int64_t nb = (static_cast<int64_t>(univ[u].n) + R - 1) / R;
+		for (int64_t I = 0; I < nb; ++I, ++s) {
+			grav_seg_desc& d = seg[s];
+			d.u = u;
+			d.il0 = static_cast<int32_t>(I * R);
+			d.unit_begin = unit;
+			d.n_units = static_cast<int32_t>(univ[u].n_jtiles - I * tpb);
+			const int64_t first = unit, last = unit + d.n_units - 1;
+			const int64_t c0 = ((first + 1) * grid + units - 1) / units - 1;
+			const int64_t c1 = ((last + 1) * grid + units - 1) / units - 1;
+			d.cta_first = static_cast<int32_t>(c0);
+			// row slots of the CTAs working on block I, then one column slot for each
+			// block before it (written by the unique-pair tiles of those blocks)
+			d.nslots = static_cast<int32_t>(c1 - c0 + 1 + I);
+			d.slot_base = static_cast<int32_t>(slots);
+			slots += d.nslots;
+			unit += d.n_units;
+		}
+	}
+	if (slots > INT32_MAX) return fail(GRAV_E_ARG, "too many partial slots");
+	info->n_bodies = body;
+	info->n_pad_total = pad;
+	info->n_units = units;
+	info->n_univ = n_univ;
+	info->n_seg = n_seg;
+	info->n_slots = static_cast<int32_t>(slots);
+	info->itile = static_cast<int32_t>(R);
+	info->pad_unit = static_cast<int32_t>(R);
 	info->grid = static_cast<int32_t>(grid);
 	if (univ_out && n_univ) std::memcpy(univ_out, univ.data(), sizeof(grav_univ_desc) * n_univ);
 	if (seg_out && n_seg) std::memcpy(seg_out, seg.data(), sizeof(grav_seg_desc) * n_seg);

@@ -18,5 +18,6 @@ struct Stage1Kernel {
 // Kernel tables, one per translation unit (stage1_f32.cu, stage1_f64.cu).
 int stage1_table_f32(const Stage1Kernel** out);
 int stage1_table_f64(const Stage1Kernel** out);
+int stage1_table_sym(const Stage1Kernel** out);
 
 }  // namespace grav

@@ -1,0 +1,237 @@
+// stage1_sym.cu -- stage 1 over unique pairs (GRAV_MODE_FP32U).
+//
+// The reference's CPU kernels visit every unordered pair once and update both bodies
+// (np1.py:81-95, _lib1_/lib.c:78-114, _lib4_/lib.c:244-317: a_i -= ..., a_j += ...).
+// This kernel does the same on the GPU, which removes a third of the FMA-pipe work of
+// the all-pairs kernel (16 instead of 2 x 12 FMA-pipe operations per pair).  Arithmetic
+// per pair is the FP32 law of stage1_f32.cu:
+//     d = r_j - r_i ; r2 = |d|^2 + eps2 ; inv3 = rsqrt(r2)^3
+//     a_i += (Gm_j inv3) d ;  a_j -= (Gm_i inv3) d
+//
+// Decomposition (plan: grav_plan_pairs).  Each universe is cut into row blocks of R =
+// 32 * W * B bodies (one segment each); the work units of row block I are the j-tiles
+// (JT bodies) of blocks J >= I.  A j-tile inside block I itself is done "all pairs,
+// rows only" (every ordered pair of the block once, like stage1_f32.cu); a j-tile of a
+// block J > I is done on unique pairs: warp w holds 32 x B rows of block I, and for
+// each 32-body chunk of the tile, lane l meets body (l + s) mod 32 of the chunk at step
+// s while the chunk's column sums rotate one lane per step (shfl), so after 32 steps
+// every row of the warp has met every body of the chunk once and each lane holds the
+// complete column sum of "its" body.  Warps add their column sums into shared memory
+// (atomics), and the tile's column sums go, as FP64, into the column slot of (I, J):
+// block J's segment lists its row slots first and then one column slot per block
+// I < J, so stage 2 adds them like any partial sums (fixed order, deterministic).
+// Row sums are FP32 per tile and folded into FP64, as in stage1_f32.cu.
+#include "grav_device.cuh"
+
+namespace grav {
+
+template <int B, int W, int JT>
+__global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
+{
+	constexpr int T = 32 * W;
+	constexpr int R = T * B;            // rows per block (= itile)
+	constexpr int TPB = R / JT;         // j-tiles per block
+	constexpr int NCH = JT / 32;        // 32-body chunks per j-tile
+	constexpr uint32_t TILE_BYTES = JT * sizeof(float4);
+	static_assert(R % JT == 0 && JT % 32 == 0, "tile shapes");
+	extern __shared__ __align__(128) float4 sym_tiles[];   // [2][JT]
+	__shared__ float colacc[3][JT];
+	__shared__ __align__(8) uint64_t bar[2];
+
+	const int tid = threadIdx.x;
+	const int lane = tid & 31;
+	const int warp = tid >> 5;
+	const int64_t U = b.n_units;
+	const int64_t G = gridDim.x;
+	const int64_t c = blockIdx.x;
+	int64_t ub = c * U / G;
+	const int64_t ue = (c + 1) * U / G;
+	if (ub >= ue) return;
+
+	for (int i = tid; i < JT; i += T) colacc[0][i] = colacc[1][i] = colacc[2][i] = 0.f;
+	if (tid == 0) {
+		mbar_init(&bar[0], 1);
+		mbar_init(&bar[1], 1);
+		fence_barrier_init();
+	}
+	__syncthreads();
+
+	const float4* __restrict__ pos = static_cast<const float4*>(b.pos);
+	const float eps2 = b.eps2;
+
+	int s;
+	{
+		int lo = 0, hi = b.n_seg - 1;
+		while (lo < hi) {
+			const int mid = (lo + hi + 1) >> 1;
+			if (b.seg[mid].unit_begin <= ub) lo = mid;
+			else hi = mid - 1;
+		}
+		s = lo;
+	}
+
+	uint32_t gt = 0;
+	bool timed_out = false;
+	while (ub < ue && s < b.n_seg) {
+		const grav_seg_desc S = b.seg[s];
+		if (S.n_units == 0 || S.unit_begin + S.n_units <= ub) {
+			++s;
+			continue;
+		}
+		const grav_univ_desc Uu = b.univ[S.u];
+		const int blkI = S.il0 / R;
+		const int64_t t0 = ub - S.unit_begin;                              // local unit
+		const int64_t t1 = min(ue - S.unit_begin, (int64_t)S.n_units);
+		const int nt = static_cast<int>(t1 - t0);
+		const int64_t jt_first = static_cast<int64_t>(blkI) * TPB;       // global j-tile of unit 0
+		const float4* __restrict__ jsrc = pos + Uu.pad_off;
+
+		if (tid == 0) {
+			const int bs = gt & 1;
+			mbar_arrive_expect_tx(&bar[bs], TILE_BYTES);
+			bulk_g2s(sym_tiles + bs * JT, jsrc + (jt_first + t0) * JT, TILE_BYTES, &bar[bs]);
+		}
+
+		// rows of this warp: w*32*B + k*32 + lane
+		const int64_t ibase = Uu.pad_off + S.il0 + warp * 32 * B + lane;
+		float xi[B], yi[B], zi[B], gi[B], fx[B], fy[B], fz[B];
+		double ax[B], ay[B], az[B];
+#pragma unroll
+		for (int k = 0; k < B; ++k) {
+			const float4 p = pos[ibase + k * 32];
+			xi[k] = p.x;
+			yi[k] = p.y;
+			zi[k] = p.z;
+			gi[k] = p.w;
+			fx[k] = fy[k] = fz[k] = 0.f;
+			ax[k] = ay[k] = az[k] = 0.0;
+		}
+
+		for (int t = 0; t < nt; ++t, ++gt) {
+			const int bs = gt & 1;
+			const bool ok = mbar_wait_bounded(&bar[bs], (gt >> 1) & 1);
+			if (__syncthreads_or(!ok)) {
+				timed_out = true;
+				break;
+			}
+			const int64_t jt = jt_first + t0 + t;  // global j-tile index in the universe
+			if (tid == 0 && t + 1 < nt) {
+				const int bn = (gt + 1) & 1;
+				mbar_arrive_expect_tx(&bar[bn], TILE_BYTES);
+				bulk_g2s(sym_tiles + bn * JT, jsrc + (jt + 1) * JT, TILE_BYTES, &bar[bn]);
+			}
+			const float4* __restrict__ sj = sym_tiles + bs * JT;
+			const int blkJ = static_cast<int>(jt / TPB);
+			if (blkJ == blkI) {
+				// diagonal block: every ordered pair of the block once, rows only
+#pragma unroll 4
+				for (int j = 0; j < JT; ++j) {
+					const float4 pj = sj[j];
+#pragma unroll
+					for (int k = 0; k < B; ++k) {
+						const float dx = pj.x - xi[k], dy = pj.y - yi[k], dz = pj.z - zi[k];
+						const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+						const float inv = rsqrt_sfu(r2);
+						float w = pj.w * inv;
+						w = w * (inv * inv);
+						fx[k] = fmaf(dx, w, fx[k]);
+						fy[k] = fmaf(dy, w, fy[k]);
+						fz[k] = fmaf(dz, w, fz[k]);
+					}
+				}
+			} else {
+				// unique pairs with block J > I: rotate the chunk's column sums
+#pragma unroll 1
+				for (int cc = 0; cc < NCH; ++cc) {
+					const int ch = (cc + warp) & (NCH - 1);
+					const float4* __restrict__ sc = sj + ch * 32;
+					float cx = 0.f, cy = 0.f, cz = 0.f;
+#pragma unroll 4
+					for (int st = 0; st < 32; ++st) {
+						const float4 pj = sc[(lane + st) & 31];
+#pragma unroll
+						for (int k = 0; k < B; ++k) {
+							const float dx = pj.x - xi[k], dy = pj.y - yi[k], dz = pj.z - zi[k];
+							const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+							const float inv = rsqrt_sfu(r2);
+							const float inv3 = inv * (inv * inv);
+							const float wj = pj.w * inv3;
+							const float wi = gi[k] * inv3;
+							fx[k] = fmaf(dx, wj, fx[k]);
+							fy[k] = fmaf(dy, wj, fy[k]);
+							fz[k] = fmaf(dz, wj, fz[k]);
+							cx = fmaf(-dx, wi, cx);
+							cy = fmaf(-dy, wi, cy);
+							cz = fmaf(-dz, wi, cz);
+						}
+						const int src = (lane + 1) & 31;
+						cx = __shfl_sync(0xffffffffu, cx, src);
+						cy = __shfl_sync(0xffffffffu, cy, src);
+						cz = __shfl_sync(0xffffffffu, cz, src);
+					}
+					atomicAdd(&colacc[0][ch * 32 + lane], cx);
+					atomicAdd(&colacc[1][ch * 32 + lane], cy);
+					atomicAdd(&colacc[2][ch * 32 + lane], cz);
+				}
+				__syncthreads();
+				// column sums of this tile -> column slot of (I, J), then clear
+				const int sJ = s + (blkJ - blkI);
+				const grav_seg_desc SJ = b.seg[sJ];
+				const int64_t slot = SJ.slot_base + SJ.nslots - (blkJ - blkI);
+				double* __restrict__ out = b.part + slot * 3 * R + (jt * JT - static_cast<int64_t>(blkJ) * R);
+				for (int i = tid; i < JT; i += T) {
+					out[i] = static_cast<double>(colacc[0][i]);
+					out[R + i] = static_cast<double>(colacc[1][i]);
+					out[2 * R + i] = static_cast<double>(colacc[2][i]);
+					colacc[0][i] = colacc[1][i] = colacc[2][i] = 0.f;
+				}
+			}
+#pragma unroll
+			for (int k = 0; k < B; ++k) {
+				ax[k] += static_cast<double>(fx[k]);
+				ay[k] += static_cast<double>(fy[k]);
+				az[k] += static_cast<double>(fz[k]);
+				fx[k] = fy[k] = fz[k] = 0.f;
+			}
+		}
+		if (timed_out) break;
+
+		const int64_t slot = S.slot_base + (c - S.cta_first);
+		double* __restrict__ out = b.part + slot * 3 * R;
+		const int r0 = warp * 32 * B + lane;
+#pragma unroll
+		for (int k = 0; k < B; ++k) {
+			out[r0 + k * 32] = ax[k];
+			out[R + r0 + k * 32] = ay[k];
+			out[2 * R + r0 + k * 32] = az[k];
+		}
+		ub = S.unit_begin + t1;
+		++s;
+	}
+
+	if (timed_out && tid == 0) {
+		set_error(b.err, GRAV_DEV_TIMEOUT);
+		mbar_wait_bounded(&bar[gt & 1], (gt >> 1) & 1);
+	}
+}
+
+#define GRAV_SYM_ENTRY(B, W, J) \
+	{GRAV_MODE_FP32U, B, 32 * W, J, reinterpret_cast<const void*>(&stage1_sym_kernel<B, W, J>), \
+		2 * J * 16}
+
+static const Stage1Kernel k_table_sym[] = {
+	GRAV_SYM_ENTRY(4, 4, 128),
+	GRAV_SYM_ENTRY(4, 8, 256),
+	GRAV_SYM_ENTRY(8, 4, 256),
+	GRAV_SYM_ENTRY(4, 4, 256),
+	GRAV_SYM_ENTRY(2, 8, 256),
+	GRAV_SYM_ENTRY(8, 8, 256),
+};
+
+int stage1_table_sym(const Stage1Kernel** out)
+{
+	*out = k_table_sym;
+	return static_cast<int>(sizeof(k_table_sym) / sizeof(k_table_sym[0]));
+}
+
+}  // namespace grav

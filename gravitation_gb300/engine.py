@@ -73,19 +73,21 @@ def occupancy(mode, tile, device=None):
     return out.value
 
 
-def make_plan(sizes, T, tile):
-    """Host-side plan (no GPU needed): (PlanInfo, univ ctypes array, seg ctypes array)."""
+def make_plan(sizes, T, tile, mode='fp32'):
+    """Host-side plan (no GPU needed): (PlanInfo, univ ctypes array, seg ctypes array).
+    The unique-pair mode (fp32u) uses grav_plan_pairs, every other mode grav_plan."""
     L = _lib.load()
+    fn = L.grav_plan_pairs if mode in ('fp32u', _lib.GRAV_MODE_FP32U) else L.grav_plan
     sizes = [int(x) for x in sizes]
     nu = len(sizes)
     n_arr = (ctypes.c_int32 * max(nu, 1))(*sizes)
     T_list = list(T) if np.ndim(T) else [float(T)] * nu
     T_arr = (ctypes.c_double * max(nu, 1))(*[float(x) for x in T_list])
     info = _lib.PlanInfo()
-    check(L.grav_plan(nu, n_arr, T_arr, ctypes.byref(tile), ctypes.byref(info), None, None))
+    check(fn(nu, n_arr, T_arr, ctypes.byref(tile), ctypes.byref(info), None, None))
     univ = (_lib.UnivDesc * max(info.n_univ, 1))()
     seg = (_lib.SegDesc * max(info.n_seg, 1))()
-    check(L.grav_plan(nu, n_arr, T_arr, ctypes.byref(tile), ctypes.byref(info), univ, seg))
+    check(fn(nu, n_arr, T_arr, ctypes.byref(tile), ctypes.byref(info), univ, seg))
     return info, univ, seg
 
 
@@ -110,7 +112,7 @@ def default_tile(mode, sizes, device=None):
             continue
         grid = info.sm_count * occ
         t.grid = grid
-        pinfo, _, _ = make_plan(sizes, 1.0, t)
+        pinfo, _, _ = make_plan(sizes, 1.0, t, mode)
         if pinfo.n_units == 0:
             continue
         # padded work (interactions) and the slowest CTA's share of it
@@ -160,7 +162,7 @@ class Engine:
         if not self.lib.grav_tile_supported(self.mode, ctypes.byref(tile)):
             raise ValueError('tile %r is not compiled for mode %s' % (tile, self.mode_name))
         self.tile = tile
-        self.info, univ, seg = make_plan(self.sizes, self.T, tile)
+        self.info, univ, seg = make_plan(self.sizes, self.T, tile, self.mode_name)
         info = self.info
         dev = self.device
         self.univ_dev = _ctypes_to_device(univ, ctypes.sizeof(_lib.UnivDesc) * info.n_univ, dev)
@@ -262,21 +264,34 @@ class Engine:
         return self.a[:self.info.n_bodies, :3]
 
     # ---- diagnostics ----------------------------------------------------------------
+    DIAG_TILE = (2, 128, 128)
+
     def _fp64_view(self):
-        """An FP64-mode batch sharing r, v and the plan, with its own padded double4
+        """An FP64-mode batch sharing r and v, with its own all-pairs plan, padded double4
         positions and partial-sum scratch (so a diagnostic never clobbers stage 1)."""
         if getattr(self, '_b64', None) is None:
-            info = self.info
+            t = _lib.Tile(*self.DIAG_TILE, 0)
+            t.grid = self.dev_info.sm_count * max(
+                occupancy(_lib.GRAV_MODE_FP64, t, self.dev_info.index), 1)
+            info, univ, seg = make_plan(self.sizes, self.T, t, 'fp64')
+            dev = self.device
+            self._univ64 = _ctypes_to_device(univ, ctypes.sizeof(_lib.UnivDesc) * info.n_univ, dev)
+            self._seg64 = _ctypes_to_device(seg, ctypes.sizeof(_lib.SegDesc) * info.n_seg, dev)
             nbytes = int(self.lib.grav_pos_bytes(_lib.GRAV_MODE_FP64, info.n_pad_total))
-            self._pos64 = torch.zeros(max(nbytes // 8, 4), dtype=torch.float64, device=self.device)
-            self._part64 = torch.zeros_like(self.part)
-            self._out64 = torch.zeros(max(info.n_univ, 1) * 8, dtype=torch.float64,
-                                      device=self.device)
+            self._pos64 = torch.zeros(max(nbytes // 8, 4), dtype=torch.float64, device=dev)
+            self._part64 = torch.zeros(max(int(self.lib.grav_part_bytes(ctypes.byref(info))) // 8,
+                                           1), dtype=torch.float64, device=dev)
+            self._out64 = torch.zeros(max(info.n_univ, 1) * 8, dtype=torch.float64, device=dev)
             b = _lib.Batch()
-            ctypes.pointer(b)[0] = self.batch
             b.mode = _lib.GRAV_MODE_FP64
-            b.pos = self._pos64.data_ptr()
-            b.part = self._part64.data_ptr()
+            b.n_univ, b.n_seg, b.n_slots = info.n_univ, info.n_seg, info.n_slots
+            b.n_bodies, b.n_pad_total, b.n_units = info.n_bodies, info.n_pad_total, info.n_units
+            b.tile = _lib.Tile(t.bpt, t.threads, t.jtile, info.grid)
+            b.eps2 = 1e-30
+            b.univ, b.seg = self._univ64.data_ptr(), self._seg64.data_ptr()
+            b.r, b.v = self.r.data_ptr(), self.v.data_ptr()
+            b.pos, b.part = self._pos64.data_ptr(), self._part64.data_ptr()
+            b.a_out, b.err = self.a.data_ptr(), self.err.data_ptr()
             self._b64 = b
         return self._b64
 

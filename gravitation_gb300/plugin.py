@@ -16,8 +16,9 @@ Behaviour seen from the front end (README.md:50, worker.py:119-136):
     kernels re-read pm._r every stage 1 (np1.py:101-102, pc2.py:147-151).
 
 Kernel options (keyword arguments of the constructor, kept in self._meta):
-  precision  'fp32' | 'fp32c' | 'fp64'   default from dtype ('float32'->fp32,
-             'float64'->fp64)
+  precision  'fp32u' | 'fp32' | 'fp32c' | 'fp64'   default from dtype
+             ('float32'->fp32u, 'float64'->fp64); fp32u and fp32 share the FP32
+             arithmetic, fp32u visits each pair once (faster), fp32 all ordered pairs
   host_sync  'full' (upload + download every step) | 'pull' (download only) |
              'none' (device state only; call sync_host() to refresh the mirror)
   fuse       True (default): stage 1 and stage 2 both run in step_stage1 on the GPU
@@ -34,7 +35,9 @@ import torch
 from . import _lib
 from .engine import Engine
 
-_DTYPE_MODE = {'float32': 'fp32', 'float64': 'fp64'}
+# float32 runs the unique-pair FP32 kernel (same FP32 arithmetic as 'fp32', each pair
+# visited once like the reference's CPU kernels); 'fp32' selects the all-pairs kernel
+_DTYPE_MODE = {'float32': 'fp32u', 'float64': 'fp64'}
 
 
 class GB300Stages:

@@ -50,6 +50,8 @@ extern "C" {
 #define GRAV_MODE_FP32 0      /* FP32 separations and weights, FP32 tile partials summed in FP64 */
 #define GRAV_MODE_FP32C 1     /* as FP32 with double-single (hi+lo) positions: separations exact */
 #define GRAV_MODE_FP64 2      /* FP64 throughout */
+#define GRAV_MODE_FP32U 3     /* FP32 arithmetic of GRAV_MODE_FP32 on unique pairs (each pair
+                                 once, both bodies updated); plan with grav_plan_pairs */
 
 /* stage-2 flags */
 #define GRAV_S2_INTEGRATE 1   /* v = a*T + v ; r = v*T + r */
@@ -152,6 +154,17 @@ int grav_occupancy(int mode, const grav_tile* tile, int32_t* ctas_per_sm);
  * pc2.py:99-145); the work list has no reference counterpart.
  */
 int grav_plan(int32_t n_univ, const int32_t* n, const double* T, const grav_tile* tile,
+	grav_plan_info* info, grav_univ_desc* univ_out, grav_seg_desc* seg_out);
+
+/*
+ * Plan for GRAV_MODE_FP32U (same protocol and outputs as grav_plan).  Universes are cut
+ * into row blocks of bpt*threads bodies (segments); the units of block I are the
+ * j-tiles of blocks J >= I.  Segment J's slots are its row slots followed by one column
+ * slot per block I < J.  Requires threads >= 32 and bpt*threads a multiple of jtile.
+ * Replaces the unique-pair row partition of the reference's CPU kernels
+ * (np1.py:104-105, _lib1_/lib.c:70-124, _lib4_/lib.c:76-144).
+ */
+int grav_plan_pairs(int32_t n_univ, const int32_t* n, const double* T, const grav_tile* tile,
 	grav_plan_info* info, grav_univ_desc* univ_out, grav_seg_desc* seg_out);
 
 /* Bytes of the padded stage-1 position array for `mode` and `n_pad_total` rows. */

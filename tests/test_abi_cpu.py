@@ -115,6 +115,77 @@ def test_plan_covers_every_unit_once(L, sizes, tile):
         assert sorted(slots) == list(range(info.n_slots))
 
 
+@pytest.mark.parametrize('sizes,tile', [
+    ([1], (4, 128, 128, 8)),
+    ([1000], (4, 128, 128, 300)),
+    ([65536], (4, 256, 256, 304)),
+    ([5, 0, 3000, 129, 2048], (8, 128, 256, 40)),
+    ([64, 16384, 77, 1000, 3000], (2, 256, 256, 1216)),
+])
+def test_pairs_plan_covers_every_pair_once(L, sizes, tile):
+    """Walk grav_plan_pairs the way stage1_sym_kernel does: every row slot is written by
+    exactly one CTA, and every column-slot entry of a real body exactly once."""
+    t = _lib.Tile(*tile)
+    info, univ, seg = make_plan(sizes, 1.0, t, 'fp32u')
+    R, JT = t.bpt * t.threads, t.jtile
+    TPB = R // JT
+    assert info.itile == R and info.n_pad_total == info.n_seg * R
+    segs = [seg[i] for i in range(info.n_seg)]
+    if info.n_units == 0:
+        return
+    U, G = info.n_units, info.grid
+    begins = [s.unit_begin for s in segs]
+    written = {}
+    pairs_seen = {}
+    for c in range(G):
+        ub, ue = c * U // G, (c + 1) * U // G
+        s = max(i for i, b in enumerate(begins) if b <= ub)
+        while ub < ue and s < len(segs):
+            S = segs[s]
+            if S.n_units == 0 or S.unit_begin + S.n_units <= ub:
+                s += 1
+                continue
+            blkI = S.il0 // R
+            t0, t1 = ub - S.unit_begin, min(ue - S.unit_begin, S.n_units)
+            for tt in range(t0, t1):
+                jt = blkI * TPB + tt
+                blkJ = jt // TPB
+                key = (S.u, blkI, jt)
+                pairs_seen[key] = pairs_seen.get(key, 0) + 1
+                if blkJ != blkI:
+                    SJ = segs[s + blkJ - blkI]
+                    assert SJ.u == S.u and SJ.il0 == blkJ * R
+                    slot = SJ.slot_base + SJ.nslots - (blkJ - blkI)
+                    assert SJ.slot_base <= slot < SJ.slot_base + SJ.nslots
+                    off = jt * JT - blkJ * R
+                    for e in range(off, off + JT):
+                        written[(slot, e)] = written.get((slot, e), 0) + 1
+            slot = S.slot_base + (c - S.cta_first)
+            assert (slot, 'row') not in written
+            written[(slot, 'row')] = 1
+            ub = S.unit_begin + t1
+            s += 1
+    assert all(v == 1 for v in pairs_seen.values())
+    assert all(v == 1 for v in written.values())
+    # every slot a real body sums in stage 2 was written
+    for si, S in enumerate(segs):
+        n = sizes[S.u]
+        nrow = S.nslots - S.il0 // R
+        for k in range(S.nslots):
+            slot = S.slot_base + k
+            if k < nrow:
+                assert (slot, 'row') in written
+            else:
+                for e in range(R):
+                    if S.il0 + e < n:
+                        assert (slot, e) in written, (si, k, e)
+    # units: j-tiles from the row block onwards, real tiles only
+    for u, n in enumerate(sizes):
+        nb = -(-n // R)
+        tiles = [k for k in pairs_seen if k[0] == u]
+        assert len(tiles) == sum(univ[u].n_jtiles - I * TPB for I in range(nb))
+
+
 def test_plan_rejects_bad_input(L):
     info = _lib.PlanInfo()
     n = (ctypes.c_int32 * 2)(5, -1)

@@ -21,7 +21,7 @@ from gravitation_gb300.scenarios import G_DEFAULT, uniform_cube, plummer_pair
 
 pytestmark = pytest.mark.gpu
 
-TOL = {'fp32': 1e-5, 'fp32c': 1e-5, 'fp64': 1e-12}
+TOL = {'fp32': 1e-5, 'fp32u': 1e-5, 'fp32c': 1e-5, 'fp64': 1e-12}
 
 
 def r32(r):
@@ -30,7 +30,7 @@ def r32(r):
 
 def oracle_accel(mode, r, m, G, rows=None):
     """FP64 oracle on the state the mode is compared against (see module doc)."""
-    if mode == 'fp32':
+    if mode in ('fp32', 'fp32u'):
         gm32 = (G * np.asarray(m)).astype(np.float32).astype(np.float64)
         return oracle.accel_fp64(r32(r), gm32, 1.0, rows=rows, coincident=True)
     return oracle.accel_fp64(r, G * np.asarray(m), 1.0, rows=rows, coincident=True)
@@ -44,7 +44,7 @@ def engine_forces(mode, r, v, m, G=G_DEFAULT, tile=None):
     return a, eng
 
 
-@pytest.mark.parametrize('mode', ['fp32', 'fp32c', 'fp64'])
+@pytest.mark.parametrize('mode', ['fp32', 'fp32u', 'fp32c', 'fp64'])
 @pytest.mark.parametrize('n', [1, 2, 3, 31, 33, 127, 129, 257, 1000])
 def test_forces_small_n(gpu, mode, n):
     r, v, m = uniform_cube(n, seed=100 + n)
@@ -57,7 +57,7 @@ def test_forces_small_n(gpu, mode, n):
     assert err.max() < TOL[mode], (mode, n, err.max())
 
 
-@pytest.mark.parametrize('mode', ['fp32', 'fp32c', 'fp64'])
+@pytest.mark.parametrize('mode', ['fp32', 'fp32u', 'fp32c', 'fp64'])
 def test_every_tile_shape(gpu, mode):
     n = 777
     r, v, m = uniform_cube(n, seed=7)
@@ -148,7 +148,7 @@ def test_full_size_sampled_65536(gpu):
     n = 65536
     r, v, m = uniform_cube(n, seed=0)
     rows = np.random.default_rng(9).choice(n, 192, replace=False)
-    for mode in ('fp32', 'fp32c'):
+    for mode in ('fp32', 'fp32u', 'fp32c'):
         a, _ = engine_forces(mode, r, v, m)
         ref = oracle_accel(mode, r, m, G_DEFAULT, rows=rows)
         err = oracle.rel_err_per_body(a[rows], ref)
@@ -175,13 +175,33 @@ def test_size_independent_properties_65536(gpu):
     assert oracle.rel_err_per_body(a3, a1).max() < 2e-6
 
 
+def test_unique_pairs_matches_all_pairs_65536(gpu):
+    """The unique-pair kernel (fp32u) against the all-pairs kernel (fp32) at N = 65536:
+    same FP32 arithmetic per pair, different summation order."""
+    n = 65536
+    r, v, m = uniform_cube(n, seed=0)
+    rows = np.random.default_rng(19).choice(n, 256, replace=False)
+    ref = oracle_accel('fp32u', r, m, G_DEFAULT, rows=rows)
+    a_all, _ = engine_forces('fp32', r, v, m)
+    a_u, eng = engine_forces('fp32u', r, v, m)
+    # both within 1e-5 of the FP64 oracle, hence within 1e-5 of each other
+    assert oracle.rel_err_per_body(a_u, a_all).max() < 1e-5
+    assert np.array_equal(a_u, eng.forces().cpu().numpy())   # deterministic
+    p = (m[:, None] * a_u).sum(0)
+    assert np.linalg.norm(p) < 1e-6 * (m * np.linalg.norm(a_u, axis=1)).sum()
+    for t in tile_list('fp32u'):
+        a_t, _ = engine_forces('fp32u', r, v, m, tile=_lib.Tile(t.bpt, t.threads, t.jtile, 0))
+        assert oracle.rel_err_per_body(a_t[rows], ref).max() < 1e-5, t
+        assert oracle.rel_err_per_body(a_t, a_all).max() < 1e-5, t
+
+
 def test_plummer_pair_precision_modes(gpu):
     """Clustered input far from the origin: fp32c and fp64 hold their bounds on the
     FP64 state; plain fp32 holds its bound on the positions it reads."""
     n = 4096
     r, v, m = plummer_pair(n, seed=2)
     rows = np.arange(0, n, 16)
-    for mode in ('fp32', 'fp32c', 'fp64'):
+    for mode in ('fp32', 'fp32u', 'fp32c', 'fp64'):
         a, _ = engine_forces(mode, r, v, m)
         ref = oracle_accel(mode, r, m, G_DEFAULT, rows=rows)
         err = oracle.rel_err_per_body(a[rows], ref).max()
@@ -199,7 +219,7 @@ def test_edge_cases(gpu):
     # coincident bodies exert no force on each other (the reference gives inf/nan)
     r = np.array([[0.0, 0, 0], [1.0, 0, 0], [1.0, 0, 0]])
     m = np.ones(3) / G_DEFAULT
-    for mode in ('fp32', 'fp32c', 'fp64'):
+    for mode in ('fp32', 'fp32u', 'fp32c', 'fp64'):
         a, _ = engine_forces(mode, r, np.zeros((3, 3)), m)
         assert np.all(np.isfinite(a))
         assert np.allclose(a[1], [-1.0, 0, 0], rtol=1e-6)
@@ -219,7 +239,7 @@ def test_batched_matches_single(gpu):
     """Several universes in one persistent launch == each universe alone."""
     sizes = [64, 1000, 3, 4096, 517]
     rs, vs, ms = zip(*[uniform_cube(n, seed=50 + i) for i, n in enumerate(sizes)])
-    for mode in ('fp32', 'fp64'):
+    for mode in ('fp32', 'fp32u', 'fp64'):
         eng = Engine(sizes, [1e3] * len(sizes), mode=mode)
         eng.set_state(np.concatenate(rs), np.concatenate(vs), G_DEFAULT * np.concatenate(ms))
         a = eng.forces().cpu().numpy()
@@ -235,7 +255,7 @@ def test_energy_momentum_fp64(gpu):
     """Energy and momentum of every universe of a batch against the FP64 oracle."""
     sizes = [2, 300, 1500, 77]
     rs, vs, ms = zip(*[uniform_cube(n, seed=70 + i) for i, n in enumerate(sizes)])
-    for mode in ('fp32', 'fp64'):
+    for mode in ('fp32', 'fp32u', 'fp64'):
         eng = Engine(sizes, 1e3, mode=mode)
         eng.set_state(np.concatenate(rs), np.concatenate(vs), G_DEFAULT * np.concatenate(ms))
         out = eng.energy(G_DEFAULT)
