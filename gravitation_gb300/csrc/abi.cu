@@ -331,8 +331,10 @@ int64_t grav_part_bytes(const grav_plan_info* info)
 
 float grav_eps2(double max_gm)
 {
-	// keep Gm * eps2^-3/2 <= 1e36 (FP32 max is 3.4e38) and eps2 a normal FP32 number
-	double e = 1e-30;
+	// keep eps2^-3/2 finite in FP32 (floor 1e-25 -> 3.2e37; the unique-pair kernel forms
+	// rsqrt(r2)^3 before multiplying by the masses) and Gm * eps2^-3/2 <= 1e36 (FP32 max
+	// is 3.4e38).  r2 + 1e-25 rounds to r2 for any separation above ~1.3e-9.
+	double e = 1e-25;
 	if (max_gm > 0.0) e = std::max(e, std::pow(max_gm / 1e36, 2.0 / 3.0));
 	return static_cast<float>(e);
 }

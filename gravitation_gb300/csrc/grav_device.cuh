@@ -95,6 +95,19 @@ __device__ __forceinline__ void bulk_g2s(void* dst_smem, const void* src_gmem, u
 		: "memory");
 }
 
+// Compensated accumulation (Knuth's TwoSum, "The Art of Computer Programming" vol. 2,
+// 4.2.2): hi + lo is the running sum; the rounding error of hi + x is kept exactly and
+// added to lo.  Six FP32 additions; no FP64 (which runs at ~1/75 of the FP32 rate on
+// this GPU).  Used to fold FP32 tile partials into a ~48-bit per-body sum.
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x)
+{
+	const float s = hi + x;
+	const float bp = s - hi;
+	const float e = (hi - (s - bp)) + (x - bp);
+	hi = s;
+	lo += e;
+}
+
 // Record the first error code seen by any CTA.
 __device__ __forceinline__ void set_error(int* err, int code)
 {

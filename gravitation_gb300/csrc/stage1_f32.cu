@@ -15,9 +15,10 @@
 // Per segment a CTA holds B i-bodies per thread in registers, streams its j-tiles
 // through double-buffered shared memory with 1-D bulk copies (cp.async.bulk,
 // completion on an mbarrier), sums each j-tile's contribution in FP32 and folds
-// that partial into FP64 accumulators.  The FP64 partial of the CTA's piece of the
-// segment goes to its own slot of b.part; stage 2 adds the slots in a fixed order,
-// so results do not depend on scheduling.
+// that partial into a compensated FP32 sum (TwoSum hi + lo, ~48 bits, no FP64 in the
+// loop).  The CTA's piece of the segment goes as FP64 to its own slot of b.part;
+// stage 2 adds the slots in FP64 in a fixed order, so results do not depend on
+// scheduling.
 //
 // GRAV_MODE_FP32C reads a second FP32 array with the low parts of the positions
 // (x = hi + lo) and forms d = (hi_j - hi_i) + (lo_j - lo_i): the separation is then
@@ -96,7 +97,7 @@ __global__ void __launch_bounds__(T) stage1_f32_kernel(const grav_batch b)
 		float xi[B], yi[B], zi[B];
 		float xl[B], yl[B], zl[B];
 		float fx[B], fy[B], fz[B];
-		double ax[B], ay[B], az[B];
+		float hx[B], hy[B], hz[B], lx[B], ly[B], lz[B];  // compensated per-body sums
 #pragma unroll
 		for (int k = 0; k < B; ++k) {
 			const float4 p = pos[ibase + tid + k * T];
@@ -112,7 +113,7 @@ __global__ void __launch_bounds__(T) stage1_f32_kernel(const grav_batch b)
 				xl[k] = yl[k] = zl[k] = 0.f;
 			}
 			fx[k] = fy[k] = fz[k] = 0.f;
-			ax[k] = ay[k] = az[k] = 0.0;
+			hx[k] = hy[k] = hz[k] = lx[k] = ly[k] = lz[k] = 0.f;
 		}
 
 		for (int t = 0; t < nt; ++t, ++gt) {
@@ -159,9 +160,9 @@ __global__ void __launch_bounds__(T) stage1_f32_kernel(const grav_batch b)
 			}
 #pragma unroll
 			for (int k = 0; k < B; ++k) {
-				ax[k] += static_cast<double>(fx[k]);
-				ay[k] += static_cast<double>(fy[k]);
-				az[k] += static_cast<double>(fz[k]);
+				two_sum_acc(hx[k], lx[k], fx[k]);
+				two_sum_acc(hy[k], ly[k], fy[k]);
+				two_sum_acc(hz[k], lz[k], fz[k]);
 				fx[k] = fy[k] = fz[k] = 0.f;
 			}
 		}
@@ -172,9 +173,9 @@ __global__ void __launch_bounds__(T) stage1_f32_kernel(const grav_batch b)
 		double* __restrict__ out = b.part + slot * 3 * IT;
 #pragma unroll
 		for (int k = 0; k < B; ++k) {
-			out[tid + k * T] = ax[k];
-			out[IT + tid + k * T] = ay[k];
-			out[2 * IT + tid + k * T] = az[k];
+			out[tid + k * T] = static_cast<double>(hx[k]) + static_cast<double>(lx[k]);
+			out[IT + tid + k * T] = static_cast<double>(hy[k]) + static_cast<double>(ly[k]);
+			out[2 * IT + tid + k * T] = static_cast<double>(hz[k]) + static_cast<double>(lz[k]);
 		}
 		ub = S.unit_begin + jt1;
 		++s;

@@ -20,12 +20,13 @@
 // (atomics), and the tile's column sums go, as FP64, into the column slot of (I, J):
 // block J's segment lists its row slots first and then one column slot per block
 // I < J, so stage 2 adds them like any partial sums (fixed order, deterministic).
-// Row sums are FP32 per tile and folded into FP64, as in stage1_f32.cu.
+// Row sums are FP32 per tile, folded into compensated (TwoSum) FP32 hi+lo sums, as in
+// stage1_f32.cu; column sums are FP32 per tile and go out as FP64.
 #include "grav_device.cuh"
 
 namespace grav {
 
-template <int B, int W, int JT>
+template <int B, int W, int JT, int UNROLL = 4>
 __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 {
 	constexpr int T = 32 * W;
@@ -95,7 +96,7 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 		// rows of this warp: w*32*B + k*32 + lane
 		const int64_t ibase = Uu.pad_off + S.il0 + warp * 32 * B + lane;
 		float xi[B], yi[B], zi[B], gi[B], fx[B], fy[B], fz[B];
-		double ax[B], ay[B], az[B];
+		float hx[B], hy[B], hz[B], lx[B], ly[B], lz[B];  // compensated row sums
 #pragma unroll
 		for (int k = 0; k < B; ++k) {
 			const float4 p = pos[ibase + k * 32];
@@ -104,7 +105,7 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 			zi[k] = p.z;
 			gi[k] = p.w;
 			fx[k] = fy[k] = fz[k] = 0.f;
-			ax[k] = ay[k] = az[k] = 0.0;
+			hx[k] = hy[k] = hz[k] = lx[k] = ly[k] = lz[k] = 0.f;
 		}
 
 		for (int t = 0; t < nt; ++t, ++gt) {
@@ -146,7 +147,7 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 					const int ch = (cc + warp) & (NCH - 1);
 					const float4* __restrict__ sc = sj + ch * 32;
 					float cx = 0.f, cy = 0.f, cz = 0.f;
-#pragma unroll 4
+#pragma unroll UNROLL
 					for (int st = 0; st < 32; ++st) {
 						const float4 pj = sc[(lane + st) & 31];
 #pragma unroll
@@ -188,9 +189,9 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 			}
 #pragma unroll
 			for (int k = 0; k < B; ++k) {
-				ax[k] += static_cast<double>(fx[k]);
-				ay[k] += static_cast<double>(fy[k]);
-				az[k] += static_cast<double>(fz[k]);
+				two_sum_acc(hx[k], lx[k], fx[k]);
+				two_sum_acc(hy[k], ly[k], fy[k]);
+				two_sum_acc(hz[k], lz[k], fz[k]);
 				fx[k] = fy[k] = fz[k] = 0.f;
 			}
 		}
@@ -201,9 +202,9 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 		const int r0 = warp * 32 * B + lane;
 #pragma unroll
 		for (int k = 0; k < B; ++k) {
-			out[r0 + k * 32] = ax[k];
-			out[R + r0 + k * 32] = ay[k];
-			out[2 * R + r0 + k * 32] = az[k];
+			out[r0 + k * 32] = static_cast<double>(hx[k]) + static_cast<double>(lx[k]);
+			out[R + r0 + k * 32] = static_cast<double>(hy[k]) + static_cast<double>(ly[k]);
+			out[2 * R + r0 + k * 32] = static_cast<double>(hz[k]) + static_cast<double>(lz[k]);
 		}
 		ub = S.unit_begin + t1;
 		++s;

@@ -173,9 +173,11 @@ int64_t grav_pos_bytes(int mode, int64_t n_pad_total);
 /* Bytes of the FP64 partial-sum buffer for a plan. */
 int64_t grav_part_bytes(const grav_plan_info* info);
 
-/* r^2 floor for the FP32 modes: the smallest value that keeps G*m * r^-3 finite in
- * FP32 for the largest G*m.  It is far below the FP32 resolution of any separation
- * larger than ~1e-7 of the body coordinates, so it does not act as softening. */
+/* r^2 floor for the FP32 modes: max(1e-25, (max_gm / 1e36)^(2/3)), the smallest value
+ * that keeps both r^-3 and G*m * r^-3 finite in FP32 at zero separation.  r^2 + eps2
+ * rounds to r^2 for any separation above ~1.3e-9 (for max_gm <= 0.03), far below the
+ * FP32 resolution of the coordinates of any realistic universe, so it does not act as
+ * softening: it only makes zero-separation terms vanish (their d is exactly 0). */
 float grav_eps2(double max_gm);
 
 /* ---- stages (device work, asynchronous on `stream`) ---------------------------- */

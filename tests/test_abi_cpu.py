@@ -233,10 +233,13 @@ def test_eps2_keeps_self_term_finite(L):
         e = L.grav_eps2(gm)
         assert e > 1.17549435e-38                 # a normal FP32 number
         inv = np.float32(1.0) / np.sqrt(np.float32(e))
-        w = np.float32(gm) * inv * inv * inv
-        assert np.isfinite(w)
+        inv3 = inv * (inv * inv)                  # the unique-pair kernel's order
+        assert np.isfinite(inv3)
+        assert np.isfinite(np.float32(gm) * inv3)
+        assert np.isfinite(np.float32(gm) * inv * (inv * inv))
     # far below the FP32 resolution of a unit-size separation
     assert L.grav_eps2(1.0) < 1e-20
+    assert np.float32(1e-12) + np.float32(L.grav_eps2(6.7e-9)) == np.float32(1e-12)
 
 
 def test_pos_and_part_bytes(L):

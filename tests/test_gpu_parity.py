@@ -224,6 +224,15 @@ def test_edge_cases(gpu):
         assert np.all(np.isfinite(a))
         assert np.allclose(a[1], [-1.0, 0, 0], rtol=1e-6)
         assert np.allclose(a[0], [2.0, 0, 0], rtol=1e-6)
+    # coincident bodies far apart in the body order (different row blocks of the
+    # unique-pair kernel, so they meet on its unique-pair path, not the diagonal one)
+    r, v, m = uniform_cube(5000, seed=31)
+    r[4321] = r[7]
+    for mode in ('fp32', 'fp32u', 'fp32c', 'fp64'):
+        a, _ = engine_forces(mode, r, v, m)
+        assert np.all(np.isfinite(a)), mode
+        ref = oracle_accel(mode, r, m, G_DEFAULT, rows=np.array([7, 4321, 0]))
+        assert oracle.rel_err_per_body(a[[7, 4321, 0]], ref).max() < TOL[mode], mode
     # massless bodies feel forces but exert none
     r, v, m = uniform_cube(100, seed=3)
     m[::3] = 0.0
