@@ -58,6 +58,8 @@ def parse():
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-batched', action='store_true')
     ap.add_argument('--no-adjoint', action='store_true')
+    ap.add_argument('--workload', default=None, choices=('precision', 'sweep', 'adjoint'),
+                    help='run one secondary workload instead of the headline step')
     ap.add_argument('--profile', action='store_true',
                     help='only set up the workload and run --steps stage-1 launches '
                          '(for ncu captures); prints nothing on success')
@@ -431,10 +433,38 @@ def read_profile_traffic(mode):
     return None
 
 
+def run_workload(args):
+    """Secondary workloads, one JSON line each: precision (Plummer pair, 3 modes,
+    energy/momentum drift), sweep (N = 2^4 .. 2^17), adjoint (forward+adjoint)."""
+    import torch
+    torch.cuda.set_device(0)
+    from gravitation_gb300 import workloads
+    from gravitation_gb300.tune import default_tuner
+    if args.workload == 'precision':
+        import oracle
+
+        def check(r, gm, a, rows):
+            ref = oracle.accel_fp64(r, gm, 1.0, rows=rows, coincident=True)
+            return oracle.rel_err_per_body(a[rows], ref).max()
+        res = workloads.run_precision(n=args.n if args.n != 65536 else 16384,
+                                      steps=args.steps, check=check)
+    elif args.workload == 'sweep':
+        res = {'sweep': workloads.run_sweep(mode=args.mode, tuner=default_tuner())}
+    elif args.workload == 'adjoint':
+        res = workloads.run_adjoint(tuner=default_tuner())
+    else:
+        raise SystemExit('unknown workload %r' % args.workload)
+    res['workload_name'] = args.workload
+    print(json.dumps(res))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == 'reference':
         return run_reference(args)
+    if args.workload:
+        return run_workload(args)
     return run_ours(args)
 
 

@@ -58,6 +58,94 @@ def run_adjoint(n=4096, steps=1000, every=32, seed=3, reps=3, tuner=None, device
     }
 
 
+def run_precision(n=16384, steps=10000, every=100, seed=2, modes=('fp32u', 'fp32c', 'fp64'),
+                  sample=256, check=None, device=None):
+    """Precision stress: two Plummer spheres (scale radius 50, centres 1000 apart,
+    approaching at 5 along x, masses log-uniform in [0.1, 1000]).  For each mode: the
+    per-body acceleration error at the first and the last step, measured by
+    ``check(r, gm, a, rows)`` (the caller's reference, e.g. an FP64 all-pairs sum) on
+    sampled bodies, and the relative drift of the FP64 energy and momentum every
+    `every` steps.  Returns a dict per mode."""
+    from .scenarios import plummer_pair
+    r, v, m = plummer_pair(n, seed=seed)
+    gm = G_DEFAULT * m
+    dev = torch.device('cuda', torch.cuda.current_device() if device is None else device)
+    rows = np.random.default_rng(seed).choice(n, min(sample, n), replace=False)
+    out = {'workload': 'Plummer pair N=%d seed %d, %d steps, T=%g' % (n, seed, steps, T_DEFAULT)}
+    finals = {}
+    for mode in modes:
+        eng = Engine([n], T_DEFAULT, mode=mode, device=dev.index)
+        eng.set_state(r, v, gm)
+        errs = []
+        e0 = eng.energy(G_DEFAULT)[0]
+        E0 = e0[0] + e0[1]
+        P0 = e0[2:5]
+        pscale = float((m * np.linalg.norm(v, axis=1)).sum())
+        drift_e, drift_p = [], []
+
+        def accel_err():
+            if check is None:
+                return None
+            rs = eng.r[:n, :3].cpu().numpy()
+            a = eng.forces().cpu().numpy()
+            return float(check(rs, gm, a, rows))
+        errs.append(accel_err())
+        graph = eng.capture_graph(every)
+        t0 = time.perf_counter()
+        done = 0
+        while done < steps:
+            graph.replay()
+            done += every
+            e = eng.energy(G_DEFAULT)[0]
+            drift_e.append(abs((e[0] + e[1]) - E0) / abs(E0))
+            drift_p.append(float(np.linalg.norm(e[2:5] - P0)) / pscale)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        errs.append(accel_err())
+        finals[mode] = eng.r[:n, :3].cpu().numpy()
+        eng.raise_on_device_error()
+        out[mode] = {'accel_err_first': errs[0], 'accel_err_last': errs[1],
+                     'energy_drift_max': max(drift_e), 'energy_drift_final': drift_e[-1],
+                     'momentum_drift_max': max(drift_p), 'wall_s': wall, 'steps': done,
+                     'energy_every': every}
+    if 'fp64' in finals:
+        ref = finals['fp64']
+        scale = np.abs(ref).max()
+        for mode in modes:
+            if mode != 'fp64':
+                out[mode]['final_pos_dev_vs_fp64_rel'] = float(np.abs(finals[mode] - ref).max() / scale)
+    return out
+
+
+def run_sweep(sizes=None, mode='fp32u', reps=5, tuner=None, device=None):
+    """Interactions/s of the single-universe step over an N sweep (2^4 .. 2^17)."""
+    from .scenarios import uniform_cube
+    sizes = sizes or [2 ** k for k in range(4, 18)]
+    dev = torch.device('cuda', torch.cuda.current_device() if device is None else device)
+    stream = torch.cuda.current_stream(dev)
+    res = []
+    for n in sizes:
+        r, v, m = uniform_cube(n, seed=0)
+        eng = Engine([n], T_DEFAULT, mode=mode, tuner=tuner, device=dev.index)
+        eng.set_state(r, v, G_DEFAULT * m)
+        g = eng.capture_graph(1)
+        for _ in range(3):
+            g.replay()
+        e0, e1 = _events(1)[0]
+        k = max(reps, int(2e10 // (n * n)) if n < 8192 else reps)
+        k = min(k, 2000)
+        e0.record(stream)
+        for _ in range(k):
+            g.replay()
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / k
+        res.append({'n': n, 'ms_per_step': ms, 'interactions_per_s': n * n / (ms * 1e-3),
+                    'tile': [eng.tile.bpt, eng.tile.threads, eng.tile.jtile, eng.info.grid]})
+        eng.raise_on_device_error()
+    return res
+
+
 def _events(n):
     return [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
             for _ in range(n)]
