@@ -40,7 +40,8 @@ METRIC = ('pair-interactions/s/GPU at N=65536 and fwd+adjoint steps/s at ≤1e-5
 UNIT = 'interactions/s'
 FLOP_PER_INTERACTION = 20
 STAGE1_KERNEL = {'fp32': 'stage1_f32_kernel<FP32>', 'fp32c': 'stage1_f32_kernel<FP32C>',
-                 'fp64': 'stage1_f64_kernel', 'fp32u': 'stage1_sym_kernel'}
+                 'fp64': 'stage1_f64_kernel', 'fp32u': 'stage1_sym_kernel<NP=1>',
+                 'fp32cu': 'stage1_sym_kernel<NP=2>'}
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -51,7 +52,8 @@ def parse():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', choices=('ours', 'reference'), default='ours')
     ap.add_argument('--n', type=int, default=65536)
-    ap.add_argument('--mode', default='fp32u', choices=('fp32', 'fp32u', 'fp32c', 'fp64'))
+    ap.add_argument('--mode', default='fp32u',
+                    choices=('fp32', 'fp32u', 'fp32c', 'fp32cu', 'fp64'))
     ap.add_argument('--cpu-seconds', type=float, default=4.0,
                     help='target seconds per CPU-baseline sample run (3 runs)')
     ap.add_argument('--no-cpu', action='store_true')

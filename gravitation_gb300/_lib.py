@@ -29,8 +29,10 @@ GRAV_S2_INTEGRATE = 1
 GRAV_S2_WRITE_A = 2
 GRAV_S2_PREPARE = 4
 
+GRAV_MODE_FP32CU = 4
 MODES = {'fp32': GRAV_MODE_FP32, 'fp32c': GRAV_MODE_FP32C, 'fp64': GRAV_MODE_FP64,
-         'fp32u': GRAV_MODE_FP32U}
+         'fp32u': GRAV_MODE_FP32U, 'fp32cu': GRAV_MODE_FP32CU}
+PAIR_MODES = ('fp32u', 'fp32cu', GRAV_MODE_FP32U, GRAV_MODE_FP32CU)
 
 
 class GravError(RuntimeError):

@@ -45,7 +45,7 @@ int cuda_fail(cudaError_t e, const char* what)
 int stage1_table_for(int mode, const grav::Stage1Kernel** tab)
 {
 	if (mode == GRAV_MODE_FP64) return grav::stage1_table_f64(tab);
-	if (mode == GRAV_MODE_FP32U) return grav::stage1_table_sym(tab);
+	if (mode == GRAV_MODE_FP32U || mode == GRAV_MODE_FP32CU) return grav::stage1_table_sym(tab);
 	return grav::stage1_table_f32(tab);
 }
 
@@ -63,7 +63,7 @@ const grav::Stage1Kernel* find_kernel(int mode, int bpt, int threads, int jtile)
 bool valid_mode(int mode)
 {
 	return mode == GRAV_MODE_FP32 || mode == GRAV_MODE_FP32C || mode == GRAV_MODE_FP64 ||
-		mode == GRAV_MODE_FP32U;
+		mode == GRAV_MODE_FP32U || mode == GRAV_MODE_FP32CU;
 }
 
 int check_batch(const grav_batch* b)
@@ -319,7 +319,7 @@ int64_t grav_pos_bytes(int mode, int64_t n_pad_total)
 {
 	if (!valid_mode(mode) || n_pad_total < 0) return fail(GRAV_E_ARG, "bad mode or size");
 	if (mode == GRAV_MODE_FP64) return n_pad_total * 32;
-	if (mode == GRAV_MODE_FP32C) return n_pad_total * 32;
+	if (mode == GRAV_MODE_FP32C || mode == GRAV_MODE_FP32CU) return n_pad_total * 32;
 	return n_pad_total * 16;
 }
 

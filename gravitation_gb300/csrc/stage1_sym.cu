@@ -26,7 +26,10 @@
 
 namespace grav {
 
-template <int B, int W, int JT, int UNROLL = 4>
+// NP = 1: FP32 positions (GRAV_MODE_FP32U).  NP = 2: FP32 hi and lo parts of the FP64
+// positions (GRAV_MODE_FP32CU): d = (hi_j - hi_i) + (lo_j - lo_i), exact to FP32
+// relative precision however far from the origin the bodies are (+6 FADD per pair).
+template <int B, int W, int JT, int UNROLL = 4, int NP = 1>
 __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 {
 	constexpr int T = 32 * W;
@@ -35,7 +38,8 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 	constexpr int NCH = JT / 32;        // 32-body chunks per j-tile
 	constexpr uint32_t TILE_BYTES = JT * sizeof(float4);
 	static_assert(R % JT == 0 && JT % 32 == 0, "tile shapes");
-	extern __shared__ __align__(128) float4 sym_tiles[];   // [2][JT]
+	static_assert(NP == 1 || NP == 2, "one or two position arrays");
+	extern __shared__ __align__(128) float4 sym_tiles[];   // [2 buffers][NP][JT]
 	__shared__ float colacc[3][JT];
 	__shared__ __align__(8) uint64_t bar[2];
 
@@ -86,16 +90,21 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 		const int nt = static_cast<int>(t1 - t0);
 		const int64_t jt_first = static_cast<int64_t>(blkI) * TPB;       // global j-tile of unit 0
 		const float4* __restrict__ jsrc = pos + Uu.pad_off;
+		const float4* __restrict__ jsrclo = pos + b.n_pad_total + Uu.pad_off;
 
 		if (tid == 0) {
 			const int bs = gt & 1;
-			mbar_arrive_expect_tx(&bar[bs], TILE_BYTES);
-			bulk_g2s(sym_tiles + bs * JT, jsrc + (jt_first + t0) * JT, TILE_BYTES, &bar[bs]);
+			mbar_arrive_expect_tx(&bar[bs], NP * TILE_BYTES);
+			bulk_g2s(sym_tiles + bs * NP * JT, jsrc + (jt_first + t0) * JT, TILE_BYTES, &bar[bs]);
+			if (NP == 2)
+				bulk_g2s(sym_tiles + (bs * NP + 1) * JT, jsrclo + (jt_first + t0) * JT, TILE_BYTES,
+					&bar[bs]);
 		}
 
 		// rows of this warp: w*32*B + k*32 + lane
 		const int64_t ibase = Uu.pad_off + S.il0 + warp * 32 * B + lane;
 		float xi[B], yi[B], zi[B], gi[B], fx[B], fy[B], fz[B];
+		float xl[B], yl[B], zl[B];                       // low parts (NP == 2)
 		float hx[B], hy[B], hz[B], lx[B], ly[B], lz[B];  // compensated row sums
 #pragma unroll
 		for (int k = 0; k < B; ++k) {
@@ -104,6 +113,14 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 			yi[k] = p.y;
 			zi[k] = p.z;
 			gi[k] = p.w;
+			if (NP == 2) {
+				const float4 q = pos[b.n_pad_total + ibase + k * 32];
+				xl[k] = q.x;
+				yl[k] = q.y;
+				zl[k] = q.z;
+			} else {
+				xl[k] = yl[k] = zl[k] = 0.f;
+			}
 			fx[k] = fy[k] = fz[k] = 0.f;
 			hx[k] = hy[k] = hz[k] = lx[k] = ly[k] = lz[k] = 0.f;
 		}
@@ -118,19 +135,30 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 			const int64_t jt = jt_first + t0 + t;  // global j-tile index in the universe
 			if (tid == 0 && t + 1 < nt) {
 				const int bn = (gt + 1) & 1;
-				mbar_arrive_expect_tx(&bar[bn], TILE_BYTES);
-				bulk_g2s(sym_tiles + bn * JT, jsrc + (jt + 1) * JT, TILE_BYTES, &bar[bn]);
+				mbar_arrive_expect_tx(&bar[bn], NP * TILE_BYTES);
+				bulk_g2s(sym_tiles + bn * NP * JT, jsrc + (jt + 1) * JT, TILE_BYTES, &bar[bn]);
+				if (NP == 2)
+					bulk_g2s(sym_tiles + (bn * NP + 1) * JT, jsrclo + (jt + 1) * JT, TILE_BYTES,
+						&bar[bn]);
 			}
-			const float4* __restrict__ sj = sym_tiles + bs * JT;
+			const float4* __restrict__ sj = sym_tiles + bs * NP * JT;
+			const float4* __restrict__ sjl = sj + JT;  // low parts (NP == 2)
 			const int blkJ = static_cast<int>(jt / TPB);
 			if (blkJ == blkI) {
 				// diagonal block: every ordered pair of the block once, rows only
 #pragma unroll 4
 				for (int j = 0; j < JT; ++j) {
 					const float4 pj = sj[j];
+					float4 lj = make_float4(0.f, 0.f, 0.f, 0.f);
+					if (NP == 2) lj = sjl[j];
 #pragma unroll
 					for (int k = 0; k < B; ++k) {
-						const float dx = pj.x - xi[k], dy = pj.y - yi[k], dz = pj.z - zi[k];
+						float dx = pj.x - xi[k], dy = pj.y - yi[k], dz = pj.z - zi[k];
+						if (NP == 2) {
+							dx = dx + (lj.x - xl[k]);
+							dy = dy + (lj.y - yl[k]);
+							dz = dz + (lj.z - zl[k]);
+						}
 						const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
 						const float inv = rsqrt_sfu(r2);
 						float w = pj.w * inv;
@@ -146,13 +174,21 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 				for (int cc = 0; cc < NCH; ++cc) {
 					const int ch = (cc + warp) & (NCH - 1);
 					const float4* __restrict__ sc = sj + ch * 32;
+					const float4* __restrict__ scl = sjl + ch * 32;
 					float cx = 0.f, cy = 0.f, cz = 0.f;
 #pragma unroll UNROLL
 					for (int st = 0; st < 32; ++st) {
 						const float4 pj = sc[(lane + st) & 31];
+						float4 lj = make_float4(0.f, 0.f, 0.f, 0.f);
+						if (NP == 2) lj = scl[(lane + st) & 31];
 #pragma unroll
 						for (int k = 0; k < B; ++k) {
-							const float dx = pj.x - xi[k], dy = pj.y - yi[k], dz = pj.z - zi[k];
+							float dx = pj.x - xi[k], dy = pj.y - yi[k], dz = pj.z - zi[k];
+							if (NP == 2) {
+								dx = dx + (lj.x - xl[k]);
+								dy = dy + (lj.y - yl[k]);
+								dz = dz + (lj.z - zl[k]);
+							}
 							const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
 							const float inv = rsqrt_sfu(r2);
 							const float inv3 = inv * (inv * inv);
@@ -217,8 +253,11 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 }
 
 #define GRAV_SYM_ENTRY(B, W, J) \
-	{GRAV_MODE_FP32U, B, 32 * W, J, reinterpret_cast<const void*>(&stage1_sym_kernel<B, W, J>), \
-		2 * J * 16}
+	{GRAV_MODE_FP32U, B, 32 * W, J, \
+		reinterpret_cast<const void*>(&stage1_sym_kernel<B, W, J, 4, 1>), 2 * J * 16}
+#define GRAV_SYMC_ENTRY(B, W, J) \
+	{GRAV_MODE_FP32CU, B, 32 * W, J, \
+		reinterpret_cast<const void*>(&stage1_sym_kernel<B, W, J, 4, 2>), 2 * 2 * J * 16}
 
 static const Stage1Kernel k_table_sym[] = {
 	GRAV_SYM_ENTRY(4, 4, 128),
@@ -227,6 +266,10 @@ static const Stage1Kernel k_table_sym[] = {
 	GRAV_SYM_ENTRY(4, 4, 256),
 	GRAV_SYM_ENTRY(2, 8, 256),
 	GRAV_SYM_ENTRY(8, 8, 256),
+	GRAV_SYMC_ENTRY(4, 4, 128),
+	GRAV_SYMC_ENTRY(8, 4, 256),
+	GRAV_SYMC_ENTRY(4, 4, 256),
+	GRAV_SYMC_ENTRY(4, 8, 256),
 };
 
 int stage1_table_sym(const Stage1Kernel** out)

@@ -32,7 +32,8 @@ __global__ void __launch_bounds__(256) stage2_kernel(const grav_batch b, const i
 		} else {
 			float4* p = static_cast<float4*>(b.pos);
 			p[g] = make_float4(0.f, 0.f, 0.f, 0.f);
-			if (b.mode == GRAV_MODE_FP32C) p[b.n_pad_total + g] = make_float4(0.f, 0.f, 0.f, 0.f);
+			if (b.mode == GRAV_MODE_FP32C || b.mode == GRAV_MODE_FP32CU)
+				p[b.n_pad_total + g] = make_float4(0.f, 0.f, 0.f, 0.f);
 		}
 		return;
 	}
@@ -75,7 +76,7 @@ __global__ void __launch_bounds__(256) stage2_kernel(const grav_batch b, const i
 		const float hy = __double2float_rn(r.y);
 		const float hz = __double2float_rn(r.z);
 		p[g] = make_float4(hx, hy, hz, __double2float_rn(r.w));
-		if (b.mode == GRAV_MODE_FP32C) {
+		if (b.mode == GRAV_MODE_FP32C || b.mode == GRAV_MODE_FP32CU) {
 			p[b.n_pad_total + g] = make_float4(
 				__double2float_rn(__dsub_rn(r.x, static_cast<double>(hx))),
 				__double2float_rn(__dsub_rn(r.y, static_cast<double>(hy))),

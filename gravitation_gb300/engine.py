@@ -77,7 +77,7 @@ def make_plan(sizes, T, tile, mode='fp32'):
     """Host-side plan (no GPU needed): (PlanInfo, univ ctypes array, seg ctypes array).
     The unique-pair mode (fp32u) uses grav_plan_pairs, every other mode grav_plan."""
     L = _lib.load()
-    fn = L.grav_plan_pairs if mode in ('fp32u', _lib.GRAV_MODE_FP32U) else L.grav_plan
+    fn = L.grav_plan_pairs if mode in _lib.PAIR_MODES else L.grav_plan
     sizes = [int(x) for x in sizes]
     nu = len(sizes)
     n_arr = (ctypes.c_int32 * max(nu, 1))(*sizes)

@@ -16,9 +16,11 @@ Behaviour seen from the front end (README.md:50, worker.py:119-136):
     kernels re-read pm._r every stage 1 (np1.py:101-102, pc2.py:147-151).
 
 Kernel options (keyword arguments of the constructor, kept in self._meta):
-  precision  'fp32u' | 'fp32' | 'fp32c' | 'fp64'   default from dtype
-             ('float32'->fp32u, 'float64'->fp64); fp32u and fp32 share the FP32
-             arithmetic, fp32u visits each pair once (faster), fp32 all ordered pairs
+  precision  'fp32' | 'fp32u' | 'fp32c' | 'fp32cu' | 'fp64'   default from dtype:
+             'float32' -> fp32 below 8192 bodies, fp32u from there on; 'float64' ->
+             fp64.  fp32/fp32u share the FP32 arithmetic (fp32u visits each pair
+             once); fp32c/fp32cu add the low parts of the positions (separations
+             exact to FP32 precision anywhere in space)
   host_sync  'full' (upload + download every step) | 'pull' (download only) |
              'none' (device state only; call sync_host() to refresh the mirror)
   fuse       True (default): stage 1 and stage 2 both run in step_stage1 on the GPU
@@ -35,9 +37,18 @@ import torch
 from . import _lib
 from .engine import Engine
 
-# float32 runs the unique-pair FP32 kernel (same FP32 arithmetic as 'fp32', each pair
-# visited once like the reference's CPU kernels); 'fp32' selects the all-pairs kernel
-_DTYPE_MODE = {'float32': 'fp32u', 'float64': 'fp64'}
+# float32 runs the FP32 arithmetic either on unique pairs (fp32u: each pair once, like
+# the reference's CPU kernels; faster from ~8k bodies on) or on all ordered pairs (fp32:
+# finer work units, faster for small universes); the results agree to FP32 rounding
+_DTYPE_MODE = {'float32': 'fp32', 'float64': 'fp64'}
+UNIQUE_PAIRS_FROM_N = 8192
+
+
+def default_mode(dtype, n):
+    mode = _DTYPE_MODE.get(str(dtype))
+    if mode == 'fp32' and n >= UNIQUE_PAIRS_FROM_N:
+        mode = 'fp32u'
+    return mode
 
 
 class GB300Stages:
@@ -45,7 +56,7 @@ class GB300Stages:
 
     def start_kernel(self):
         meta = self._meta
-        mode = meta.get('precision') or _DTYPE_MODE.get(str(self._dtype))
+        mode = meta.get('precision') or default_mode(self._dtype, len(self._mass_list))
         if mode not in _lib.MODES:
             raise ValueError('unsupported dtype/precision %r (float32, float64, fp32, fp32c, '
                              'fp64)' % (meta.get('precision') or self._dtype,))

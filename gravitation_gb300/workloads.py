@@ -58,7 +58,8 @@ def run_adjoint(n=4096, steps=1000, every=32, seed=3, reps=3, tuner=None, device
     }
 
 
-def run_precision(n=16384, steps=10000, every=100, seed=2, modes=('fp32u', 'fp32c', 'fp64'),
+def run_precision(n=16384, steps=10000, every=100, seed=2,
+                  modes=('fp32u', 'fp32cu', 'fp32c', 'fp64'),
                   sample=256, check=None, device=None):
     """Precision stress: two Plummer spheres (scale radius 50, centres 1000 apart,
     approaching at 5 along x, masses log-uniform in [0.1, 1000]).  For each mode: the

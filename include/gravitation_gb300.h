@@ -52,6 +52,8 @@ extern "C" {
 #define GRAV_MODE_FP64 2      /* FP64 throughout */
 #define GRAV_MODE_FP32U 3     /* FP32 arithmetic of GRAV_MODE_FP32 on unique pairs (each pair
                                  once, both bodies updated); plan with grav_plan_pairs */
+#define GRAV_MODE_FP32CU 4    /* GRAV_MODE_FP32C's double-single positions on unique pairs;
+                                 plan with grav_plan_pairs */
 
 /* stage-2 flags */
 #define GRAV_S2_INTEGRATE 1   /* v = a*T + v ; r = v*T + r */

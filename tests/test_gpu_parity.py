@@ -21,7 +21,7 @@ from gravitation_gb300.scenarios import G_DEFAULT, uniform_cube, plummer_pair
 
 pytestmark = pytest.mark.gpu
 
-TOL = {'fp32': 1e-5, 'fp32u': 1e-5, 'fp32c': 1e-5, 'fp64': 1e-12}
+TOL = {'fp32': 1e-5, 'fp32u': 1e-5, 'fp32c': 1e-5, 'fp32cu': 1e-5, 'fp64': 1e-12}
 
 
 def r32(r):
@@ -44,7 +44,7 @@ def engine_forces(mode, r, v, m, G=G_DEFAULT, tile=None):
     return a, eng
 
 
-@pytest.mark.parametrize('mode', ['fp32', 'fp32u', 'fp32c', 'fp64'])
+@pytest.mark.parametrize('mode', ['fp32', 'fp32u', 'fp32c', 'fp32cu', 'fp64'])
 @pytest.mark.parametrize('n', [1, 2, 3, 31, 33, 127, 129, 257, 1000])
 def test_forces_small_n(gpu, mode, n):
     r, v, m = uniform_cube(n, seed=100 + n)
@@ -57,7 +57,7 @@ def test_forces_small_n(gpu, mode, n):
     assert err.max() < TOL[mode], (mode, n, err.max())
 
 
-@pytest.mark.parametrize('mode', ['fp32', 'fp32u', 'fp32c', 'fp64'])
+@pytest.mark.parametrize('mode', ['fp32', 'fp32u', 'fp32c', 'fp32cu', 'fp64'])
 def test_every_tile_shape(gpu, mode):
     n = 777
     r, v, m = uniform_cube(n, seed=7)
@@ -148,7 +148,7 @@ def test_full_size_sampled_65536(gpu):
     n = 65536
     r, v, m = uniform_cube(n, seed=0)
     rows = np.random.default_rng(9).choice(n, 192, replace=False)
-    for mode in ('fp32', 'fp32u', 'fp32c'):
+    for mode in ('fp32', 'fp32u', 'fp32c', 'fp32cu'):
         a, _ = engine_forces(mode, r, v, m)
         ref = oracle_accel(mode, r, m, G_DEFAULT, rows=rows)
         err = oracle.rel_err_per_body(a[rows], ref)
@@ -201,7 +201,7 @@ def test_plummer_pair_precision_modes(gpu):
     n = 4096
     r, v, m = plummer_pair(n, seed=2)
     rows = np.arange(0, n, 16)
-    for mode in ('fp32', 'fp32u', 'fp32c', 'fp64'):
+    for mode in ('fp32', 'fp32u', 'fp32c', 'fp32cu', 'fp64'):
         a, _ = engine_forces(mode, r, v, m)
         ref = oracle_accel(mode, r, m, G_DEFAULT, rows=rows)
         err = oracle.rel_err_per_body(a[rows], ref).max()
@@ -219,7 +219,7 @@ def test_edge_cases(gpu):
     # coincident bodies exert no force on each other (the reference gives inf/nan)
     r = np.array([[0.0, 0, 0], [1.0, 0, 0], [1.0, 0, 0]])
     m = np.ones(3) / G_DEFAULT
-    for mode in ('fp32', 'fp32u', 'fp32c', 'fp64'):
+    for mode in ('fp32', 'fp32u', 'fp32c', 'fp32cu', 'fp64'):
         a, _ = engine_forces(mode, r, np.zeros((3, 3)), m)
         assert np.all(np.isfinite(a))
         assert np.allclose(a[1], [-1.0, 0, 0], rtol=1e-6)
@@ -228,7 +228,7 @@ def test_edge_cases(gpu):
     # unique-pair kernel, so they meet on its unique-pair path, not the diagonal one)
     r, v, m = uniform_cube(5000, seed=31)
     r[4321] = r[7]
-    for mode in ('fp32', 'fp32u', 'fp32c', 'fp64'):
+    for mode in ('fp32', 'fp32u', 'fp32c', 'fp32cu', 'fp64'):
         a, _ = engine_forces(mode, r, v, m)
         assert np.all(np.isfinite(a)), mode
         ref = oracle_accel(mode, r, m, G_DEFAULT, rows=np.array([7, 4321, 0]))

@@ -121,6 +121,14 @@ def test_base_restatement_matches_reference():
                 u.stop()
 
 
+def test_default_precision_by_dtype_and_size():
+    from gravitation_gb300.plugin import default_mode
+    assert default_mode('float32', 1024) == 'fp32'
+    assert default_mode('float32', 65536) == 'fp32u'
+    assert default_mode('float64', 65536) == 'fp64'
+    assert default_mode('float16', 10) is None
+
+
 def test_default_stage2_matches_oracle():
     import oracle
     from gravitation_gb300.kernel._base_ import universe_base
