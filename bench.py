@@ -201,7 +201,9 @@ def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
         return 0
-    value, threads, sample = cpu_baseline_run(args.n, 0, args.cpu_seconds, runs=args.steps)
+    # each step is one bounded sample; keep the whole --steps run within ~2 minutes
+    target = min(args.cpu_seconds, max(0.3, 120.0 / max(1, args.steps)))
+    value, threads, sample = cpu_baseline_run(args.n, 0, target, runs=max(1, args.steps))
     line = {
         'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': UNIT,
         'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,

@@ -94,29 +94,71 @@ class AdjointEngine:
 class Rollout:
     """Forward engine + adjoint engine for one batch of universes (reusable)."""
 
-    def __init__(self, sizes, T, steps, every=32, device=None, fwd_tile=None, tuner=None):
+    def __init__(self, sizes, T, steps, every=32, device=None, fwd_tile=None, tuner=None,
+                 mode='fp32', graphs=True):
         self.sizes = [int(n) for n in sizes]
         self.T = float(T)
         self.steps = int(steps)
         self.every = max(1, int(every))
-        self.fwd = Engine(self.sizes, self.T, mode='fp32', tile=fwd_tile, device=device,
+        self.fwd = Engine(self.sizes, self.T, mode=mode, tile=fwd_tile, device=device,
                           tuner=tuner)
         self.adj = AdjointEngine(self.sizes, self.T, device=device)
+        self.graphs = bool(graphs)
+        self._fwd_graphs = {}
+        self._adj_graphs = {}
+        n = self.fwd.info.n_bodies
+        nseg = -(-self.steps // self.every)
+        # FP64 state at the start of every segment, plus the final state
+        self.ck_r = torch.zeros((nseg + 1, n, 4), dtype=torch.float64, device=self.fwd.device)
+        self.ck_v = torch.zeros_like(self.ck_r)
         self.checkpoints = []
+
+    def _segments(self):
+        starts = list(range(0, self.steps, self.every))
+        return [(s, min(s + self.every, self.steps)) for s in starts]
+
+    def _fwd_steps(self, c, stream):
+        if not self.graphs:
+            self.fwd.step(c, stream=stream)
+            return
+        g = self._fwd_graphs.get(c)
+        if g is None:
+            g = self._fwd_graphs[c] = self.fwd.capture_graph(c)
+        g.replay()
+
+    def _adj_steps(self, c, stream):
+        a = self.adj
+        if not self.graphs:
+            for _ in range(c):
+                a.step(stream)
+            return
+        g = self._adj_graphs.get(c)
+        if g is None:
+            side = torch.cuda.Stream(device=a.device)
+            side.wait_stream(torch.cuda.current_stream(a.device))
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=side):
+                for _ in range(c):
+                    a.step(side)
+            torch.cuda.current_stream(a.device).wait_stream(side)
+            self._adj_graphs[c] = g
+        g.replay()
 
     def forward(self, r0, v0, gm, stream=None):
         """Run the steps; keep the FP64 state at the start of every segment.
-        Returns device views (r[n,3], v[n,3]) of the final state."""
+        Returns device views (r[n,3], v[n,3]) of the final state.  With graphs=True each
+        segment's steps replay from a CUDA graph (captured on first use)."""
         n = self.fwd.info.n_bodies
         self.fwd.set_state(r0, v0, gm, stream=stream)
-        self.checkpoints = []
-        k = 0
-        while k < self.steps:
-            self.checkpoints.append((self.fwd.r[:n].clone(), self.fwd.v[:n].clone()))
-            c = min(self.every, self.steps - k)
-            self.fwd.step(c, stream=stream)
-            k += c
-        self.final = (self.fwd.r[:n].clone(), self.fwd.v[:n].clone())
+        segs = self._segments()
+        for si, (s0, s1) in enumerate(segs):
+            self.ck_r[si].copy_(self.fwd.r[:n])
+            self.ck_v[si].copy_(self.fwd.v[:n])
+            self._fwd_steps(s1 - s0, stream)
+        self.ck_r[len(segs)].copy_(self.fwd.r[:n])
+        self.ck_v[len(segs)].copy_(self.fwd.v[:n])
+        self.checkpoints = [(self.ck_r[i], self.ck_v[i]) for i in range(len(segs))]
+        self.final = (self.ck_r[len(segs)], self.ck_v[len(segs)])
         return self.fwd.r[:n, :3], self.fwd.v[:n, :3]
 
     def backward(self, g_r, g_v, stream=None):
@@ -128,14 +170,13 @@ class Rollout:
         a.ggm.zero_()
         a.gr[:n, :3].copy_(g_r)
         a.gv[:n, :3].copy_(g_v)
-        starts = list(range(0, self.steps, self.every))
-        for si in reversed(range(len(starts))):
-            end = starts[si + 1] if si + 1 < len(starts) else self.steps
-            state = self.checkpoints[si + 1] if si + 1 < len(starts) else self.final
-            a.set_state(*state)
+        segs = self._segments()
+        for si in reversed(range(len(segs))):
+            s0, s1 = segs[si]
+            # the exact stored state at the segment's end (the final state for the last)
+            a.set_state(self.ck_r[si + 1], self.ck_v[si + 1])
             a.prepare(stream)
-            for _ in range(end - starts[si]):
-                a.step(stream)
+            self._adj_steps(s1 - s0, stream)
         self.reversed_state = (a.r[:n, :3].clone(), a.v[:n, :3].clone())
         return a.gr[:n, :3].clone(), a.gv[:n, :3].clone(), a.ggm[:n].clone()
 

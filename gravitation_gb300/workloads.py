@@ -28,34 +28,46 @@ def run_adjoint(n=4096, steps=1000, every=32, seed=3, reps=3, tuner=None, device
     gm_t = torch.tensor(G_DEFAULT * m * mass_perturbation(n, seed), device=dev)
     r0 = torch.tensor(r, device=dev)
     v0 = torch.tensor(v, device=dev)
-    ro = Rollout([n], T_DEFAULT, steps, every, device=dev.index, tuner=tuner)
-    rt, _ = ro.forward(r0, v0, gm_t)
-    rt = rt.clone()
     stream = torch.cuda.current_stream(dev)
-    fwd_ms, tot_ms = [], []
-    for _ in range(reps):
-        e0, e1 = _events(1)[0]
-        e2 = torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        e0.record(stream)
-        rK, _ = ro.forward(r0, v0, gm)
-        e1.record(stream)
-        g_r = (2.0 / n) * (rK - rt)
-        ro.backward(g_r, torch.zeros_like(g_r))
-        e2.record(stream)
-        e2.synchronize()
-        fwd_ms.append(e0.elapsed_time(e1))
-        tot_ms.append(e0.elapsed_time(e2))
-    ro.adj.raise_on_device_error()
-    ro.fwd.raise_on_device_error()
-    f, t = min(fwd_ms), min(tot_ms)
-    return {
-        'workload': 'N=%d uniform cube seed %d, %d steps, checkpoint every %d, loss = mean '
-                    '|r_K - r_target|^2 (target: masses x U[0.99,1.01])' % (n, seed, steps, every),
-        'forward_ms': f, 'forward_adjoint_ms': t, 'ratio_fwd_plus_adjoint_over_fwd': t / f,
-        'fwd_adjoint_steps_per_s': steps / (t * 1e-3),
-        'launches_per_step': {'forward': 2, 'adjoint': 2},
-    }
+
+    def measure(graphs):
+        ro = Rollout([n], T_DEFAULT, steps, every, device=dev.index, tuner=tuner,
+                     graphs=graphs)
+        rt, _ = ro.forward(r0, v0, gm_t)
+        rt = rt.clone()
+        fwd_ms, tot_ms = [], []
+        for _ in range(reps + 1):            # the first round captures the graphs
+            e0, e1 = _events(1)[0]
+            e2 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            rK, _ = ro.forward(r0, v0, gm)
+            e1.record(stream)
+            g_r = (2.0 / n) * (rK - rt)
+            ro.backward(g_r, torch.zeros_like(g_r))
+            e2.record(stream)
+            e2.synchronize()
+            fwd_ms.append(e0.elapsed_time(e1))
+            tot_ms.append(e0.elapsed_time(e2))
+        ro.adj.raise_on_device_error()
+        ro.fwd.raise_on_device_error()
+        f, t = min(fwd_ms[1:]), min(tot_ms[1:])
+        return {'forward_ms': f, 'forward_adjoint_ms': t,
+                'ratio_fwd_plus_adjoint_over_fwd': t / f,
+                'fwd_adjoint_steps_per_s': steps / (t * 1e-3),
+                'forward_tile': [ro.fwd.tile.bpt, ro.fwd.tile.threads, ro.fwd.tile.jtile,
+                                 ro.fwd.info.grid]}
+
+    out = {'workload': 'N=%d uniform cube seed %d, %d steps, checkpoint every %d, loss = mean '
+                       '|r_K - r_target|^2 (target: masses x U[0.99,1.01])' % (n, seed, steps,
+                                                                             every),
+           'launches_per_step': {'forward': 2, 'adjoint': 2}}
+    out['graphs'] = measure(True)
+    out['launched'] = measure(False)
+    out.update({k: out['graphs'][k] for k in ('forward_ms', 'forward_adjoint_ms',
+                                             'ratio_fwd_plus_adjoint_over_fwd',
+                                             'fwd_adjoint_steps_per_s')})
+    return out
 
 
 def run_precision(n=16384, steps=10000, every=100, seed=2,
