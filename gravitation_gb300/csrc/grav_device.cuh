@@ -73,14 +73,15 @@ __device__ __forceinline__ uint64_t global_ns()
 // Bounded wait on one phase of an mbarrier.  Returns false when the phase has not
 // completed after GRAV_WAIT_NS nanoseconds of polling (the clock is read every 16
 // polls, so the bound holds whatever each poll's hardware suspend time is).
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
+	uint64_t limit_ns = GRAV_WAIT_NS)
 {
 	if (mbar_try_wait(bar, parity)) return true;
 	const uint64_t t0 = global_ns();
 	for (;;) {
 		for (int k = 0; k < 16; ++k)
 			if (mbar_try_wait(bar, parity)) return true;
-		if (global_ns() - t0 > GRAV_WAIT_NS) return false;
+		if (global_ns() - t0 > limit_ns) return false;
 	}
 }
 

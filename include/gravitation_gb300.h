@@ -284,6 +284,14 @@ int grav_adjoint_step(const grav_adjoint* a, void* stream);
 int grav_forces_noalloc(const double* r, double* a, int32_t n, double max_gm, int32_t* err,
 	void* stream);
 
+/* ---- failure path check -------------------------------------------------------------- */
+
+/* Test hook: one CTA waits, with the library's bounded wait and a limit of `limit_ns`
+ * (<= 2e9), on an mbarrier that nothing completes, then writes GRAV_DEV_TIMEOUT to the
+ * device int `err` and returns.  Shows that an expired wait is reported to the host and
+ * leaves the context usable.  No reference counterpart. */
+int grav_wait_check(int32_t* err, int64_t limit_ns, void* stream);
+
 /* ---- measurement ------------------------------------------------------------------ */
 
 /* FP32 FMA throughput probe: `blocks` CTAs of 256 threads, each thread 8 independent
