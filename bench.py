@@ -60,7 +60,8 @@ def parse():
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-batched', action='store_true')
     ap.add_argument('--no-adjoint', action='store_true')
-    ap.add_argument('--workload', default=None, choices=('precision', 'sweep', 'adjoint'),
+    ap.add_argument('--workload', default=None,
+                    choices=('precision', 'sweep', 'adjoint', 'adjoint-check'),
                     help='run one secondary workload instead of the headline step')
     ap.add_argument('--profile', action='store_true',
                     help='only set up the workload and run --steps stage-1 launches '
@@ -456,6 +457,8 @@ def run_workload(args):
         res = {'sweep': workloads.run_sweep(mode=args.mode, tuner=default_tuner())}
     elif args.workload == 'adjoint':
         res = workloads.run_adjoint(tuner=default_tuner())
+    elif args.workload == 'adjoint-check':
+        res = workloads.run_adjoint_check()
     else:
         raise SystemExit('unknown workload %r' % args.workload)
     res['workload_name'] = args.workload

@@ -70,6 +70,78 @@ def run_adjoint(n=4096, steps=1000, every=32, seed=3, reps=3, tuner=None, device
     return out
 
 
+def run_adjoint_check(n=4096, steps=1000, every=32, seed=3, ncoords=16, eps=1e-6,
+                      device=None):
+    """Gradients of the differentiable-rollout workload (N=4096, 1000 steps, checkpoint
+    every 32) against FP64 central finite differences with step eps on `ncoords` seeded
+    coordinates of (r0, v0, m).  The finite differences run full FP64 rollouts on the
+    GPU (fp64 mode); the target is the same FP64 run with masses scaled by the seeded
+    factor in [0.99, 1.01].  Returns per-coordinate gradients and relative errors."""
+    from .adjoint import Rollout
+    from .scenarios import mass_perturbation, uniform_cube
+    r, v, m = uniform_cube(n, seed=seed)
+    f = mass_perturbation(n, seed)
+    dev = torch.device('cuda', torch.cuda.current_device() if device is None else device)
+    e64 = Engine([n], T_DEFAULT, mode='fp64', device=dev.index)
+    g64 = {}
+
+    def final64(rr, vv, mm):
+        e64.set_state(rr, vv, G_DEFAULT * mm)
+        if every not in g64:
+            g64[every] = e64.capture_graph(every)
+        done = 0
+        while done + every <= steps:
+            g64[every].replay()
+            done += every
+        if done < steps:
+            e64.step(steps - done)
+        return e64.r[:n, :3].cpu().numpy()
+
+    t = final64(r, v, m * f)
+
+    def loss(rr, vv, mm):
+        rk = final64(rr, vv, mm)
+        return float(((rk - t) ** 2).sum(1).mean())
+
+    # adjoint gradients (FP32 pairs, FP64 state) of the same loss
+    ro = Rollout([n], T_DEFAULT, steps, every, device=dev.index)
+    r0 = torch.tensor(r, device=dev)
+    v0 = torch.tensor(v, device=dev)
+    rK, _ = ro.forward(r0, v0, torch.tensor(G_DEFAULT * m, device=dev))
+    tt = torch.tensor(t, device=dev)
+    loss_adj = float(((rK - tt) ** 2).sum(1).mean())
+    g_r, g_v, g_gm = ro.backward((2.0 / n) * (rK - tt), torch.zeros_like(rK))
+    g_r, g_v = g_r.cpu().numpy(), g_v.cpu().numpy()
+    g_m = G_DEFAULT * g_gm.cpu().numpy()
+    rng = np.random.default_rng(np.random.SeedSequence([seed, 16]))
+    rows = []
+    for _ in range(ncoords):
+        which = int(rng.integers(3))
+        i = int(rng.integers(n))
+        c = int(rng.integers(3))
+        args_p = [r.copy(), v.copy(), m.copy()]
+        args_m = [r.copy(), v.copy(), m.copy()]
+        if which == 2:
+            args_p[2][i] += eps
+            args_m[2][i] -= eps
+            g = float(g_m[i])
+        else:
+            args_p[which][i, c] += eps
+            args_m[which][i, c] -= eps
+            g = float((g_r, g_v)[which][i, c])
+        fd = (loss(*args_p) - loss(*args_m)) / (2 * eps)
+        rows.append({'var': ('r0', 'v0', 'm')[which], 'body': i, 'comp': c, 'adjoint': g,
+                     'fd': fd, 'rel_err': abs(g - fd) / max(abs(fd), 1e-300)})
+    e64.raise_on_device_error()
+    errs = {k: [x['rel_err'] for x in rows if x['var'] == k] for k in ('r0', 'v0', 'm')}
+    return {'workload': 'N=%d uniform cube seed %d, %d steps, checkpoint every %d; FD eps %g '
+                        'on %d seeded coordinates' % (n, seed, steps, every, eps, ncoords),
+            'loss_fp64': loss(r, v, m), 'loss_adjoint_forward': loss_adj,
+            'max_rel_err': {k: (max(vs) if vs else None) for k, vs in errs.items()},
+            'median_rel_err': {k: (float(np.median(vs)) if vs else None) for k, vs in errs.items()},
+            'coords': rows}
+
+
 def run_precision(n=16384, steps=10000, every=100, seed=2,
                   modes=('fp32u', 'fp32cu', 'fp32c', 'fp64'),
                   sample=256, check=None, device=None):
