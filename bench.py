@@ -66,6 +66,9 @@ def parse():
     ap.add_argument('--profile', action='store_true',
                     help='only set up the workload and run --steps stage-1 launches '
                          '(for ncu captures); prints nothing on success')
+    ap.add_argument('--profile-all', action='store_true',
+                    help='with --profile: also run steps, the energy diagnostic and adjoint '
+                         'steps (for captures of those kernels)')
     ap.add_argument('--tile', default=None,
                     help='force the stage-1 tile as bpt,threads,jtile (default: autotuned)')
     a = ap.parse_args()
@@ -286,8 +289,21 @@ def run_ours(args):
     eng.set_state(r, v, gm)
     stream = torch.cuda.current_stream(device)
     if args.profile:
+        # stage 1 alone, then (for the other kernels' captures) full steps, the FP64
+        # energy diagnostic and backward adjoint steps, each --warmup + --steps times
         for _ in range(args.warmup + args.steps):
             eng.stage1()
+        if args.profile_all:
+            from gravitation_gb300.adjoint import AdjointEngine
+            adj = AdjointEngine([n], T_DEFAULT, device=local)
+            adj.set_state(eng.r[:n], eng.v[:n])
+            adj.gr[:n, :3].normal_()
+            for _ in range(args.warmup + args.steps):
+                eng.step(1)
+                eng.energy(G_DEFAULT)
+                adj.prepare()
+                adj.step()
+            adj.raise_on_device_error()
         torch.cuda.synchronize()
         eng.raise_on_device_error()
         return 0
