@@ -23,7 +23,8 @@
 // segment, so rounding in the reversal never accumulates over more than one segment.
 //
 // Pair kernel: persistent stage-1 work list (pairs_skeleton.cuh), j-tiles of FP32
-// positions (x, y, z, Gm) and FP32 u, FP32 tile partials folded into FP64; 7 outputs
+// positions (x, y, z, Gm) and FP32 u, FP32 tile partials folded into compensated
+// (TwoSum) FP32 sums, so no FP64 arithmetic runs in the pair loop; 7 outputs
 // per body (a, h, g) in the partial slots.  Adjoint stage 2 (one thread per padded row)
 // sums the slots and applies the updates above in FP64, then prepares the FP32
 // positions r_{k-1} and u for the next backward step.
@@ -41,7 +42,8 @@ struct VjpOp {
 	const float4* upos;
 	float xi[B], yi[B], zi[B], gmi[B], uxi[B], uyi[B], uzi[B];
 	float fa[3][B], fp[3][B], fq[3][B], fs[B], fg[B];
-	double da[3][B], dh[3][B], dg[B];
+	// compensated (TwoSum) running sums: high and low FP32 parts
+	float ah[3][B], al[3][B], hh[3][B], hl[3][B], gh[B], gl[B];
 
 	__device__ const Elem* jsrc(int a) const { return a == 0 ? pos : upos; }
 
@@ -61,10 +63,10 @@ struct VjpOp {
 #pragma unroll
 			for (int c = 0; c < 3; ++c) {
 				fa[c][k] = fp[c][k] = fq[c][k] = 0.f;
-				da[c][k] = dh[c][k] = 0.0;
+				ah[c][k] = al[c][k] = hh[c][k] = hl[c][k] = 0.f;
 			}
 			fs[k] = fg[k] = 0.f;
-			dg[k] = 0.0;
+			gh[k] = gl[k] = 0.f;
 		}
 	}
 
@@ -102,23 +104,23 @@ struct VjpOp {
 				fg[k] = fmaf(duj, inv3, fg[k]);
 			}
 		}
-		// fold the tile's FP32 partials into FP64
+		// fold the tile's FP32 partials into compensated FP32 (TwoSum) sums
 #pragma unroll
 		for (int k = 0; k < B; ++k) {
 #pragma unroll
 			for (int c3 = 0; c3 < 3; ++c3) {
-				da[c3][k] += static_cast<double>(fa[c3][k]);
+				two_sum_acc(ah[c3][k], al[c3][k], fa[c3][k]);
 				fa[c3][k] = 0.f;
 			}
 			const float ui[3] = {uxi[k], uyi[k], uzi[k]};
 #pragma unroll
 			for (int c3 = 0; c3 < 3; ++c3) {
 				// h = Gm_k P - u_k S + Q   (the -3 is folded into t)
-				dh[c3][k] += static_cast<double>(gmi[k]) * fp[c3][k] -
-					static_cast<double>(ui[c3]) * fs[k] + static_cast<double>(fq[c3][k]);
+				const float ht = fmaf(gmi[k], fp[c3][k], fmaf(-ui[c3], fs[k], fq[c3][k]));
+				two_sum_acc(hh[c3][k], hl[c3][k], ht);
 				fp[c3][k] = fq[c3][k] = 0.f;
 			}
-			dg[k] += static_cast<double>(fg[k]);
+			two_sum_acc(gh[k], gl[k], fg[k]);
 			fs[k] = fg[k] = 0.f;
 		}
 	}
@@ -129,13 +131,13 @@ struct VjpOp {
 #pragma unroll
 		for (int k = 0; k < B; ++k) {
 			const int i = tid + k * T;
-			out[0 * IT + i] = da[0][k];
-			out[1 * IT + i] = da[1][k];
-			out[2 * IT + i] = da[2][k];
-			out[3 * IT + i] = dh[0][k];
-			out[4 * IT + i] = dh[1][k];
-			out[5 * IT + i] = dh[2][k];
-			out[6 * IT + i] = dg[k];
+#pragma unroll
+			for (int c3 = 0; c3 < 3; ++c3) {
+				out[c3 * IT + i] = static_cast<double>(ah[c3][k]) + static_cast<double>(al[c3][k]);
+				out[(3 + c3) * IT + i] =
+					static_cast<double>(hh[c3][k]) + static_cast<double>(hl[c3][k]);
+			}
+			out[6 * IT + i] = static_cast<double>(gh[k]) + static_cast<double>(gl[k]);
 		}
 	}
 };
