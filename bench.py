@@ -417,12 +417,11 @@ def run_ours(args):
     return 0
 
 
-def run_e2e(args, r, v, m, local):
-    """gb1.universe.step() timed by wall clock, FP64 r and v crossing PCIe/C2C each step."""
-    import torch
+def _e2e_once(args, r, v, m, local, zero_copy):
     from gravitation_gb300.kernel import gb1
     n = len(m)
-    u = gb1.universe(dtype='float32', precision=args.mode, host_sync='full', device=local)
+    u = gb1.universe(dtype='float32', precision=args.mode, host_sync='full', device=local,
+                     zero_copy=zero_copy)
     for i in range(n):
         u.add_object(name='s', r=[float(r[i, 0]), float(r[i, 1]), float(r[i, 2])],
                      v=[float(v[i, 0]), float(v[i, 1]), float(v[i, 2])], m=float(m[i]))
@@ -434,11 +433,29 @@ def run_e2e(args, r, v, m, local):
         t0 = time.perf_counter()
         u.step()
         times.append(time.perf_counter() - t0)
+    used = u._gb_zero_copy
     u.stop()
-    mean = statistics.mean(times)
-    return {'value': n * n / mean, 'unit': UNIT, 'h2d_bytes_per_step': 2 * n * 32,
-            'd2h_bytes_per_step': 2 * n * 32, 'ms_per_step': 1e3 * mean,
-            'ms_per_step_min': 1e3 * min(times), 'path': 'gb1.universe.step(), host_sync=full'}
+    return times, used
+
+
+def run_e2e(args, r, v, m, local):
+    """gb1.universe.step() timed by wall clock with the FP64 state in pinned host memory
+    (the mirror pm._r / pm._v are views of), crossing the CPU-GPU link every step.
+    Default plugin path: prepare reads r and stage 2 reads and writes r, v in place in
+    host memory (h2d 96 B/body, d2h 64 B/body + the 4-byte error flag).  The copy path
+    (upload r, v; download r, v: 64 B/body each way) is timed beside it."""
+    n = len(m)
+    times, zc = _e2e_once(args, r, v, m, local, zero_copy=True)
+    copies, _ = _e2e_once(args, r, v, m, local, zero_copy=False)
+    mean, mean_c = statistics.mean(times), statistics.mean(copies)
+    return {'value': n * n / mean, 'unit': UNIT,
+            'h2d_bytes_per_step': (96 if zc else 64) * n,
+            'd2h_bytes_per_step': 64 * n + 4, 'ms_per_step': 1e3 * mean,
+            'ms_per_step_min': 1e3 * min(times),
+            'path': 'gb1.universe.step(), host_sync=full, %s' % (
+                'state in pinned host memory (zero_copy)' if zc else 'copies'),
+            'copies_path': {'value': n * n / mean_c, 'ms_per_step': 1e3 * mean_c,
+                            'h2d_bytes_per_step': 64 * n, 'd2h_bytes_per_step': 64 * n + 4}}
 
 
 def read_profile_traffic(mode):

@@ -116,6 +116,7 @@ _DECLS = {
                                             ctypes.c_void_p]),
     'grav_energy': (ctypes.c_int, [_P(Batch), ctypes.c_void_p, ctypes.c_void_p]),
     'grav_wait_check': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
+    'grav_host_device_pointer': (ctypes.c_int, [ctypes.c_void_p, _P(ctypes.c_void_p)]),
     'grav_adjoint_tile_supported': (ctypes.c_int, [_P(Tile)]),
     'grav_adjoint_occupancy': (ctypes.c_int, [_P(Tile), _P(ctypes.c_int32)]),
     'grav_adjoint_prepare': (ctypes.c_int, [_P(Adjoint), ctypes.c_void_p]),

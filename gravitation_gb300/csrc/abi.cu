@@ -392,4 +392,19 @@ int grav_step(const grav_batch* b, int flags, void* stream)
 	return grav_stage2(b, flags & ~GRAV_S2_PREPARE, stream);
 }
 
+int grav_host_device_pointer(const void* host, void** dev)
+{
+	if (!host || !dev) return fail(GRAV_E_ARG, "NULL host or dev pointer");
+	cudaPointerAttributes at;
+	cudaError_t e = cudaPointerGetAttributes(&at, host);
+	if (e != cudaSuccess) {
+		cudaGetLastError();  // not a sticky error: clear it
+		return fail(GRAV_E_ARG, "cudaPointerGetAttributes: %s", cudaGetErrorString(e));
+	}
+	if (at.type != cudaMemoryTypeHost || at.devicePointer == nullptr)
+		return fail(GRAV_E_ARG, "%p is not page-locked host memory mapped for the device", host);
+	*dev = at.devicePointer;
+	return ok();
+}
+
 }  // extern "C"

@@ -221,6 +221,27 @@ class Engine:
             self.v[:n, 3].zero_()
         self.prepare(stream)
 
+    def bind_host_state(self, hr, hv):
+        """Keep r and v in page-locked host tensors hr, hv (float64 [n_bodies, 4], same
+        layout): prepare and stage 2 then read and write them in place over the CPU-GPU
+        link, and the device copies are no longer used.  Returns False, changing
+        nothing, if the tensors are not page-locked memory the device can address."""
+        n = self.info.n_bodies
+        for t in (hr, hv):
+            if (t.device.type != 'cpu' or t.dtype != torch.float64 or tuple(t.shape) != (n, 4)
+                    or not t.is_contiguous()):
+                raise ValueError('host state must be contiguous float64 [%d, 4] CPU tensors' % n)
+        ptrs = []
+        for t in (hr, hv):
+            p = ctypes.c_void_p()
+            if not t.is_pinned() or self.lib.grav_host_device_pointer(
+                    ctypes.c_void_p(t.data_ptr()), ctypes.byref(p)) != _lib.GRAV_OK:
+                return False
+            ptrs.append(p.value)
+        self.r, self.v = hr, hv
+        self.batch.r, self.batch.v = ptrs
+        return True
+
     def _stream(self, stream):
         return stream if stream is not None else torch.cuda.current_stream(self.device)
 

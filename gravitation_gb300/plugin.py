@@ -29,6 +29,12 @@ Kernel options (keyword arguments of the constructor, kept in self._meta):
   tile       (bpt, threads, jtile) to force a tile shape; default: autotuned
   autotune   True (default) to use the autotuner cache / tuning
   device     CUDA device index (default: current device)
+  graph      True (default): with fuse, a step is one CUDA-graph replay of upload,
+             stage 1, stage 2 and download (the velocity upload overlaps stage 1);
+             False: the same work launched call by call
+  zero_copy  True (default): with host_sync='full', r and v stay in the pinned host
+             mirror, which the GPU reads and writes in place over the CPU-GPU link
+             (NVLink-C2C on Grace); False: device copies, uploaded and downloaded
 """
 
 import numpy as np
@@ -89,7 +95,9 @@ class GB300Stages:
             hv[i, :3] = pm._v[:3]
         if not np.all(np.isfinite(hr)) or not np.all(np.isfinite(hv)):
             raise ValueError('positions, velocities and masses must be finite')
+        self._gb_herr = torch.zeros(1, dtype=torch.int32, pin_memory=pin)
         self._gb_stream = torch.cuda.Stream(device=dev)
+        self._gb_side = torch.cuda.Stream(device=dev)
         self._gb.set_state(hr[:, :3], hv[:, :3], hr[:, 3], stream=self._gb_stream)
         self._gb_stream.synchronize()
         # np2-style binding: the point masses see rows of the host mirror
@@ -97,48 +105,109 @@ class GB300Stages:
             pm._r = hr[i, :3]
             pm._v = hv[i, :3]
             pm._a = ha[i, :3]
+        self._gb_a_dirty = False
+        # host_sync='full' keeps the state in the host mirror itself when the device can
+        # address it: prepare and stage 2 read and write it in place
+        self._gb_zero_copy = False
+        if self._gb_sync == 'full' and meta.get('zero_copy', True):
+            self._gb_zero_copy = self._gb.bind_host_state(self._gb_hr, self._gb_hv)
+        self._gb_graph = None
+        if self._gb_fuse and meta.get('graph', True):
+            self._gb_graph = self._gb_capture()
 
     # ---- stages ----------------------------------------------------------------------
-    def _gb_upload(self):
-        g, s = self._gb, self._gb_stream
-        with torch.cuda.stream(s):
-            g.r.copy_(self._gb_hr, non_blocking=True)
-            g.v.copy_(self._gb_hv, non_blocking=True)
-        g.prepare(stream=s)
+    def _gb_enqueue_step(self):
+        """Queue one fused step on the kernel's stream: upload (host_sync='full'),
+        stage 1, stage 2, download (full/pull) and the device error flag.  With an
+        upload, positions go first and the velocities travel on a side stream while
+        stage 1 runs (stage 1 reads only positions).  With the state in the host
+        mirror (zero_copy) prepare reads the positions and stage 2 updates r and v in
+        place, so only the error flag is copied."""
+        g, s, side = self._gb, self._gb_stream, self._gb_side
+        if self._gb_zero_copy:
+            g.prepare(stream=s)
+            g.step(1, stream=s)
+            self._gb_enqueue_download(state=False)
+            return
+        if self._gb_sync == 'full':
+            side.wait_stream(s)
+            with torch.cuda.stream(side):
+                g.v.copy_(self._gb_hv, non_blocking=True)
+            with torch.cuda.stream(s):
+                g.r.copy_(self._gb_hr, non_blocking=True)
+            g.prepare(stream=s)
+            g.stage1(stream=s)
+            s.wait_stream(side)
+            g.stage2(_lib.GRAV_S2_INTEGRATE, stream=s)
+        else:
+            g.step(1, stream=s)
+        self._gb_enqueue_download(state=self._gb_sync in ('full', 'pull'))
 
-    def _gb_download(self, with_a=False):
+    def _gb_enqueue_download(self, state=True, with_a=False):
         g, s = self._gb, self._gb_stream
         with torch.cuda.stream(s):
-            self._gb_hr.copy_(g.r, non_blocking=True)
-            self._gb_hv.copy_(g.v, non_blocking=True)
+            if state and not self._gb_zero_copy:
+                self._gb_hr.copy_(g.r, non_blocking=True)
+                self._gb_hv.copy_(g.v, non_blocking=True)
             if with_a:
                 self._gb_ha.copy_(g.a, non_blocking=True)
-        s.synchronize()
-        self._gb.raise_on_device_error()
+            self._gb_herr.copy_(g.err, non_blocking=True)
+
+    def _gb_capture(self):
+        """CUDA graph of one fused step (memory copies and kernels; the pinned host
+        mirror and the device buffers keep their addresses for the universe's life)."""
+        s = self._gb_stream
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=s):
+            self._gb_enqueue_step()
+        return graph
+
+    def _gb_finish(self):
+        """Wait for the queued work; raise on the device error flag it copied back."""
+        self._gb_stream.synchronize()
+        code = int(self._gb_herr[0])
+        if code != _lib.GRAV_DEV_OK:
+            self._gb.raise_on_device_error()
+
+    def _gb_download(self, state=True):
+        self._gb_enqueue_download(state=state)
+        self._gb_finish()
 
     def step_stage1(self):
-        if self._gb_sync == 'full':
-            self._gb_upload()
         if self._gb_fuse:
-            self._gb.step(1, stream=self._gb_stream)
-        else:
-            g, s = self._gb, self._gb_stream
-            g.stage1(stream=s)
-            g.stage2(_lib.GRAV_S2_WRITE_A, stream=s)
-            with torch.cuda.stream(s):
-                self._gb_ha.copy_(g.a, non_blocking=True)
-            s.synchronize()
-            g.raise_on_device_error()
+            if self._gb_graph is not None:
+                # replay() launches on the current stream: make it the kernel's stream,
+                # the one _gb_finish waits for
+                with torch.cuda.stream(self._gb_stream):
+                    self._gb_graph.replay()
+            else:
+                self._gb_enqueue_step()
+            return
+        g, s = self._gb, self._gb_stream
+        if self._gb_sync == 'full':
+            if not self._gb_zero_copy:
+                with torch.cuda.stream(s):
+                    g.r.copy_(self._gb_hr, non_blocking=True)
+                    g.v.copy_(self._gb_hv, non_blocking=True)
+            g.prepare(stream=s)
+        g.stage1(stream=s)
+        g.stage2(_lib.GRAV_S2_WRITE_A, stream=s)
+        self._gb_enqueue_download(state=False, with_a=True)
+        self._gb_finish()
+        self._gb_a_dirty = True
 
     def step_stage2(self):
-        if not self._gb_fuse:
-            self._gb.stage2(_lib.GRAV_S2_INTEGRATE, stream=self._gb_stream)
-        if self._gb_sync in ('full', 'pull'):
-            self._gb_download()
-        else:
-            self._gb_stream.synchronize()
-        # the base class's stage 2 leaves the accelerations zeroed (_base_.py:62)
-        self._gb_ha[:, :3] = 0.0
+        if self._gb_fuse:
+            # the step queued by step_stage1 already holds its download
+            self._gb_finish()
+            return
+        self._gb.stage2(_lib.GRAV_S2_INTEGRATE, stream=self._gb_stream)
+        self._gb_download(state=self._gb_sync in ('full', 'pull'))
+        # the base class's stage 2 leaves the accelerations zeroed (_base_.py:62);
+        # only the unfused stage 1 writes them
+        if self._gb_a_dirty:
+            self._gb_ha[:, :3] = 0.0
+            self._gb_a_dirty = False
 
     def sync_host(self):
         """Refresh the host mirror (pm._r, pm._v) from the device state."""
@@ -147,5 +216,6 @@ class GB300Stages:
     def stop_kernel(self):
         if getattr(self, '_gb', None) is not None:
             self._gb_stream.synchronize()
-            self._gb_download()
+            self.sync_host()
+            self._gb_graph = None
             self._gb = None

@@ -284,6 +284,19 @@ int grav_adjoint_step(const grav_adjoint* a, void* stream);
 int grav_forces_noalloc(const double* r, double* a, int32_t n, double max_gm, int32_t* err,
 	void* stream);
 
+/* ---- host-resident state ------------------------------------------------------------ */
+
+/*
+ * Device address of page-locked host memory (cudaHostAlloc / cudaHostRegister, e.g. a
+ * pinned PyTorch tensor).  A grav_batch whose r and v point there makes grav_prepare
+ * and grav_stage2 read and write the host copy in place over the CPU-GPU link, so a
+ * host-synchronised step needs no separate copies.  Writes *dev, or returns GRAV_E_ARG
+ * when `host` is not page-locked memory that the current device can address.
+ * No counterpart in the reference (its kernels copy numpy arrays in and out every
+ * step, np1.py:101-108, pc2.py:147-168).
+ */
+int grav_host_device_pointer(const void* host, void** dev);
+
 /* ---- failure path check -------------------------------------------------------------- */
 
 /* Test hook: one CTA waits, with the library's bounded wait and a limit of `limit_ns`

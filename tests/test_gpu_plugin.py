@@ -118,3 +118,34 @@ def test_precision_option_and_scaling(gpu, golden):
     assert oracle.rel_err_per_body(a, ref).max() < 1e-5
     # and the reference's own FP32 kernel on the same bodies
     assert np.median(oracle.rel_err_per_body(golden['gal_np1_f32_a0'], a)) < 1e-5
+
+
+@pytest.mark.parametrize('sync', ['full', 'pull', 'none'])
+def test_graph_step_matches_launched_step(gpu, sync):
+    """The graph-replayed fused step (default), the same work launched call by call,
+    the host-resident state (zero_copy, host_sync='full') and the unfused stages give
+    bit-identical states, for every host_sync mode; with 'full' an edit of the host
+    mirror between steps reaches all of them."""
+    r, v, m = uniform_cube(700, seed=8)
+    variants = [dict(graph=True), dict(graph=False)]
+    if sync == 'full':
+        variants = [dict(graph=True, zero_copy=True), dict(graph=False, zero_copy=True),
+                    dict(graph=True, zero_copy=False), dict(graph=False, zero_copy=False),
+                    dict(fuse=False, zero_copy=True), dict(fuse=False, zero_copy=False)]
+    out = []
+    for kw in variants:
+        u = make_universe(r, v, m, dtype='float32', precision='fp32u', host_sync=sync, **kw)
+        assert (u._gb_graph is not None) == (kw.get('graph', True) and kw.get('fuse', True))
+        assert u._gb_zero_copy == (sync == 'full' and kw.get('zero_copy', True))
+        for k in range(4):
+            u.step()
+            if k == 1 and sync == 'full':
+                next(iter(u))._v[:] = [0.5, -0.25, 0.0]
+        if sync == 'none':
+            u.sync_host()
+        assert all(list(pm._a) == [0.0, 0.0, 0.0] for pm in u)
+        out.append(state(u))
+        u.stop()
+    for rv in out[1:]:
+        assert np.array_equal(out[0][0], rv[0]) and np.array_equal(out[0][1], rv[1])
+    assert not np.array_equal(out[0][0], r)
