@@ -9,8 +9,9 @@ reference has no dataset, its own scenarios are generated too.
   value      pair interactions per second (N^2 per step), device-timed steps with the
              state resident in HBM; L2 flushed (256 MiB write) between timed steps
   e2e        the same metric through the reference-facing plugin (gb1.universe.step()
-             with host_sync='full'): per step the FP64 r, v are uploaded from pinned
-             host memory and downloaded back, wall-clock timed
+             with host_sync='full'): the FP64 r, v live in pinned host memory (the
+             point masses' pm._r / pm._v) and cross the CPU-GPU link every step,
+             wall-clock timed; the upload/download copy path is timed beside it
   roofline   stage-1 kernel: 20 FLOP per interaction / kernel time, against the FP32
              FMA peak measured live by grav_fp32_peak_probe (SMs x 128 x 2 x clock)
   cpu_baseline  the reference's fastest CPU design (portable restatement in
@@ -61,7 +62,7 @@ def parse():
     ap.add_argument('--no-batched', action='store_true')
     ap.add_argument('--no-adjoint', action='store_true')
     ap.add_argument('--workload', default=None,
-                    choices=('precision', 'sweep', 'adjoint', 'adjoint-check'),
+                    choices=('precision', 'sweep', 'adjoint', 'adjoint-check', 'scenario'),
                     help='run one secondary workload instead of the headline step')
     ap.add_argument('--profile', action='store_true',
                     help='only set up the workload and run --steps stage-1 launches '
@@ -74,6 +75,15 @@ def parse():
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
     return a
+
+
+def measured_peaks():
+    """The machine's measured HBM and tensor peaks (MEASURED_PEAKS.json at the repo root)."""
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
 
 
 # ---- distributed plumbing ----------------------------------------------------------------
@@ -492,6 +502,8 @@ def run_workload(args):
         res = workloads.run_adjoint(tuner=default_tuner())
     elif args.workload == 'adjoint-check':
         res = workloads.run_adjoint_check()
+    elif args.workload == 'scenario':
+        res = workloads.run_generate(hbm_gbs=measured_peaks().get('hbm_gbs'))
     else:
         raise SystemExit('unknown workload %r' % args.workload)
     res['workload_name'] = args.workload

@@ -91,6 +91,16 @@ class Adjoint(ctypes.Structure):
                 ('ggm', ctypes.c_void_p), ('upos', ctypes.c_void_p), ('part7', ctypes.c_void_p)]
 
 
+GRAV_SCEN_UNIFORM_CUBE = 1
+GRAV_SCEN_PLUMMER = 2
+GRAV_SCEN_GALAXY = 3
+
+
+class Scenario(ctypes.Structure):
+    _fields_ = [('kind', ctypes.c_int32), ('_pad0', ctypes.c_int32), ('seed', ctypes.c_uint64),
+                ('stream', ctypes.c_uint64), ('G', ctypes.c_double), ('p', ctypes.c_double * 10)]
+
+
 # ---- declarations -----------------------------------------------------------------
 _P = ctypes.POINTER
 _DECLS = {
@@ -117,6 +127,9 @@ _DECLS = {
     'grav_energy': (ctypes.c_int, [_P(Batch), ctypes.c_void_p, ctypes.c_void_p]),
     'grav_wait_check': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
     'grav_host_device_pointer': (ctypes.c_int, [ctypes.c_void_p, _P(ctypes.c_void_p)]),
+    'grav_scenario_scratch_bytes': (ctypes.c_int64, [_P(Scenario), ctypes.c_int64]),
+    'grav_scenario_generate': (ctypes.c_int, [_P(Scenario), ctypes.c_void_p, ctypes.c_void_p,
+                                              ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]),
     'grav_adjoint_tile_supported': (ctypes.c_int, [_P(Tile)]),
     'grav_adjoint_occupancy': (ctypes.c_int, [_P(Tile), _P(ctypes.c_int32)]),
     'grav_adjoint_prepare': (ctypes.c_int, [_P(Adjoint), ctypes.c_void_p]),

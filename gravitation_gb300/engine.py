@@ -221,6 +221,29 @@ class Engine:
             self.v[:n, 3].zero_()
         self.prepare(stream)
 
+    def generate_state(self, scenarios, G, stream=None):
+        """Fill r and v on the device from seeded scenarios (gravitation_gb300.generate):
+        one list of parts per universe, covering exactly that universe's bodies; G is
+        the (scaled) constant the G*m column is formed with (one per universe or one
+        for all).  Sets eps2 from the largest G*m and refreshes the stage-1 positions."""
+        from . import generate as gen
+        if len(scenarios) != len(self.sizes):
+            raise ValueError('%d scenarios for %d universes' % (len(scenarios), len(self.sizes)))
+        Gs = list(G) if np.ndim(G) else [float(G)] * len(self.sizes)
+        st = self._stream(stream)
+        for u, parts in enumerate(scenarios):
+            n = self.sizes[u]
+            if gen.total_bodies(parts) != n or sum(p.n for p in parts) != n:
+                raise ValueError('scenario of universe %d does not cover its %d bodies' % (u, n))
+            o = int(self.offsets[u])
+            gen.generate(parts, self.r[o:o + n], self.v[o:o + n], Gs[u], st)
+        nb = self.info.n_bodies
+        st.synchronize()  # r may be host memory the device wrote (bind_host_state)
+        with torch.cuda.stream(st):
+            max_gm = float(self.r[:nb, 3].max()) if nb else 0.0
+        self.batch.eps2 = float(self.lib.grav_eps2(max_gm))
+        self.prepare(st)
+
     def bind_host_state(self, hr, hv):
         """Keep r and v in page-locked host tensors hr, hv (float64 [n_bodies, 4], same
         layout): prepare and stage 2 then read and write them in place over the CPU-GPU

@@ -35,12 +35,18 @@ Kernel options (keyword arguments of the constructor, kept in self._meta):
   zero_copy  True (default): with host_sync='full', r and v stay in the pinned host
              mirror, which the GPU reads and writes in place over the CPU-GPU link
              (NVLink-C2C on Grace); False: device copies, uploaded and downloaded
+  scenario   instead of add_object calls: a dict such as {'kind': 'plummer_pair',
+             'n': 16384, 'seed': 2} or a list of gravitation_gb300.generate parts; the
+             bodies are generated on the device in the universe's scaled units and
+             the point masses are made on first access (see _MirrorMasses)
 """
+
+import sys
 
 import numpy as np
 import torch
 
-from . import _lib
+from . import _lib, generate
 from .engine import Engine
 
 # float32 runs the FP32 arithmetic either on unique pairs (fp32u: each pair once, like
@@ -57,12 +63,59 @@ def default_mode(dtype, n):
     return mode
 
 
+class _MirrorMasses:
+    """The point-mass list of a universe whose bodies were generated on the device.
+
+    Behaves as the base class's ``_mass_list`` does for its readers (``len``,
+    iteration, indexing: _base_.py:95-100): each body is a ``_point_mass`` of the
+    base class, made on first access, whose ``_r``, ``_v`` and ``_a`` are rows of the
+    pinned host mirror and whose ``_m`` is the scaled mass.  Nothing per body is
+    built before the front end asks for it."""
+
+    def __init__(self, cls, hr, hv, ha, G, parts):
+        self._cls, self._hr, self._hv, self._ha, self._G = cls, hr, hv, ha, G
+        self._items = [None] * len(hr)
+        self._names = []
+        for p in parts:
+            self._names.append((p.offset, p.offset + p.n, p.kind))
+
+    def __len__(self):
+        return len(self._items)
+
+    def __getitem__(self, i):
+        if isinstance(i, slice):
+            return [self[k] for k in range(*i.indices(len(self._items)))]
+        i = range(len(self._items))[i]
+        pm = self._items[i]
+        if pm is None:
+            name = next((k for lo, hi, k in self._names if lo <= i < hi), 'body')
+            m = float(self._hr[i, 3]) / self._G if self._G else 0.0
+            pm = self._cls(name='%s %d' % (name, i), r=self._hr[i, :3], v=self._hv[i, :3], m=m)
+            pm._a = self._ha[i, :3]
+            self._items[i] = pm
+        return pm
+
+    def __iter__(self):
+        for i in range(len(self._items)):
+            yield self[i]
+
+
 class GB300Stages:
     """start/step/stop hooks of a gravitation kernel running on one GB300."""
 
     def start_kernel(self):
         meta = self._meta
-        mode = meta.get('precision') or default_mode(self._dtype, len(self._mass_list))
+        parts = None
+        if meta.get('scenario') is not None:
+            if len(self._mass_list):
+                raise ValueError('a scenario generated on the device replaces add_object: '
+                                 'use one or the other')
+            spec = meta['scenario']
+            parts = list(spec) if isinstance(spec, (list, tuple)) else generate.from_spec(spec)
+            n = generate.total_bodies(parts)
+        else:
+            n = len(self._mass_list)
+        mode = meta.get('precision') or default_mode(self._dtype, n)
         if mode not in _lib.MODES:
             raise ValueError('unsupported dtype/precision %r (float32, float64, fp32, fp32c, '
                              'fp64)' % (meta.get('precision') or self._dtype,))
@@ -70,7 +123,6 @@ class GB300Stages:
         if self._gb_sync not in ('full', 'pull', 'none'):
             raise ValueError('host_sync must be full, pull or none')
         self._gb_fuse = bool(meta.get('fuse', True))
-        n = len(self._mass_list)
         if n == 0:
             raise ValueError('no point masses were added before start()')
         tile = meta.get('tile')
@@ -89,22 +141,32 @@ class GB300Stages:
         self._gb_hv = torch.zeros((n, 4), dtype=torch.float64, pin_memory=pin)
         self._gb_ha = torch.zeros((n, 4), dtype=torch.float64, pin_memory=pin)
         hr, hv, ha = self._gb_hr.numpy(), self._gb_hv.numpy(), self._gb_ha.numpy()
-        for i, pm in enumerate(self._mass_list):
-            hr[i, :3] = pm._r[:3]
-            hr[i, 3] = self._G * pm._m
-            hv[i, :3] = pm._v[:3]
-        if not np.all(np.isfinite(hr)) or not np.all(np.isfinite(hv)):
-            raise ValueError('positions, velocities and masses must be finite')
         self._gb_herr = torch.zeros(1, dtype=torch.int32, pin_memory=pin)
         self._gb_stream = torch.cuda.Stream(device=dev)
         self._gb_side = torch.cuda.Stream(device=dev)
-        self._gb.set_state(hr[:, :3], hv[:, :3], hr[:, 3], stream=self._gb_stream)
-        self._gb_stream.synchronize()
-        # np2-style binding: the point masses see rows of the host mirror
-        for i, pm in enumerate(self._mass_list):
-            pm._r = hr[i, :3]
-            pm._v = hv[i, :3]
-            pm._a = ha[i, :3]
+        if parts is not None:
+            # bodies written by the device, then one copy into the host mirror
+            self._gb.generate_state([parts], G=self._G, stream=self._gb_stream)
+            with torch.cuda.stream(self._gb_stream):
+                self._gb_hr.copy_(self._gb.r[:n], non_blocking=True)
+                self._gb_hv.copy_(self._gb.v[:n], non_blocking=True)
+            self._gb_stream.synchronize()
+            self._mass_list = _MirrorMasses(self._point_mass_class(), hr, hv, ha, self._G,
+                                            parts)
+        else:
+            for i, pm in enumerate(self._mass_list):
+                hr[i, :3] = pm._r[:3]
+                hr[i, 3] = self._G * pm._m
+                hv[i, :3] = pm._v[:3]
+            if not np.all(np.isfinite(hr)) or not np.all(np.isfinite(hv)):
+                raise ValueError('positions, velocities and masses must be finite')
+            self._gb.set_state(hr[:, :3], hv[:, :3], hr[:, 3], stream=self._gb_stream)
+            self._gb_stream.synchronize()
+            # np2-style binding: the point masses see rows of the host mirror
+            for i, pm in enumerate(self._mass_list):
+                pm._r = hr[i, :3]
+                pm._v = hv[i, :3]
+                pm._a = ha[i, :3]
         self._gb_a_dirty = False
         # host_sync='full' keeps the state in the host mirror itself when the device can
         # address it: prepare and stage 2 read and write it in place
@@ -114,6 +176,13 @@ class GB300Stages:
         self._gb_graph = None
         if self._gb_fuse and meta.get('graph', True):
             self._gb_graph = self._gb_capture()
+
+    def _point_mass_class(self):
+        """The ``_point_mass`` class of the module that defines this universe's base."""
+        for c in type(self).__mro__:
+            if c.__name__ == 'universe_base':
+                return getattr(sys.modules[c.__module__], '_point_mass')
+        raise TypeError('no universe_base among the bases of %r' % (type(self),))
 
     # ---- stages ----------------------------------------------------------------------
     def _gb_enqueue_step(self):

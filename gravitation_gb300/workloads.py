@@ -329,3 +329,69 @@ def run_batched(steps=100, warmup=3, mode='fp32', n_univ=256, seed=1, loop_steps
         'launches_per_step': 2,
         'loop_launches_per_step': 2 * n_univ,
     }
+
+
+def run_generate(n_big=1 << 24, n_plugin=1 << 17, reps=5, hbm_gbs=None, device=None):
+    """Scenario generation on the device (gravitation_gb300.generate).
+
+    Throughput: n_big bodies of each scenario written into device r, v (64 B per body
+    written: two rows of 4 doubles; nothing read but the Plummer's per-CTA sums), CUDA
+    events around each call, best of `reps`, against the HBM copy bandwidth.  Start-up:
+    a gb1 universe of n_plugin bodies started from a scenario against the same universe
+    built by n_plugin add_object calls with numpy-generated bodies (wall clock)."""
+    from . import generate as gen
+    from .kernel import gb1
+    from .scenarios import uniform_cube
+    dev = torch.device('cuda', torch.cuda.current_device() if device is None else device)
+    stream = torch.cuda.current_stream(dev)
+    r = torch.empty((n_big, 4), dtype=torch.float64, device=dev)
+    v = torch.empty((n_big, 4), dtype=torch.float64, device=dev)
+    out = {'n': n_big, 'bytes_written_per_body': 64}
+    cases = {'uniform_cube': gen.uniform_cube(n_big, seed=0),
+             'plummer_pair': gen.plummer_pair(n_big, seed=2),
+             'galaxy': gen.galaxy(n_big, seed=0)}
+    for name, parts in cases.items():
+        G = G_DEFAULT * (1e-10 ** 3 / 1e-30 if name == 'galaxy' else 1.0)
+        gen.generate(parts, r, v, G, stream)
+        ms = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            gen.generate(parts, r, v, G, stream)
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        best = min(ms)
+        gbs = 64.0 * n_big / (best * 1e-3) / 1e9
+        # FP64 log/exp/sin/cos per body on GB300's reduced FP64 pipe bound these
+        # kernels, not the 64 B/body of writes (fraction of HBM reported for scale)
+        out[name] = {'ms': best, 'bodies_per_s': n_big / (best * 1e-3), 'write_gbs': gbs,
+                     'hbm_frac': gbs / hbm_gbs if hbm_gbs else None,
+                     'launches': 3 * len(parts) if name == 'plummer_pair' else len(parts)}
+    del r, v
+    torch.cuda.synchronize()
+
+    # one untimed start first: the tile autotuner's first visit to this size class and
+    # the first graph capture would otherwise be charged to whichever path runs first
+    w = gb1.universe(scenario={'kind': 'uniform_cube', 'n': n_plugin, 'seed': 1})
+    w.start()
+    w.stop()
+    t0 = time.perf_counter()
+    u = gb1.universe(scenario={'kind': 'uniform_cube', 'n': n_plugin, 'seed': 0})
+    u.start()
+    t_scen = time.perf_counter() - t0
+    u.step()
+    u.stop()
+    t0 = time.perf_counter()
+    rr, vv, mm = uniform_cube(n_plugin, seed=0)
+    w = gb1.universe()
+    for i in range(n_plugin):
+        w.add_object(name='b', r=[float(rr[i, 0]), float(rr[i, 1]), float(rr[i, 2])],
+                     v=[float(vv[i, 0]), float(vv[i, 1]), float(vv[i, 2])], m=float(mm[i]))
+    t_objects = time.perf_counter() - t0
+    w.start()
+    t_add = time.perf_counter() - t0
+    w.stop()
+    out['plugin_start'] = {'n': n_plugin, 'scenario_s': t_scen, 'add_object_s': t_add,
+                           'add_object_loop_s': t_objects, 'speedup': t_add / t_scen}
+    return out

@@ -284,6 +284,61 @@ int grav_adjoint_step(const grav_adjoint* a, void* stream);
 int grav_forces_noalloc(const double* r, double* a, int32_t n, double max_gm, int32_t* err,
 	void* stream);
 
+/* ---- scenarios generated on the device ---------------------------------------------- */
+
+/* Scenario kinds (grav_scenario.kind). */
+#define GRAV_SCEN_UNIFORM_CUBE 1 /* p = {half, v_sigma, m_lo, m_hi} */
+#define GRAV_SCEN_PLUMMER 2      /* p = {a, m_lo, m_hi, cx, cy, cz, cvx, cvy, cvz} */
+#define GRAV_SCEN_GALAXY 3       /* p = {radius, m_hole, m_star, scale_r, scale_m} */
+
+/*
+ * A seeded scenario.  Random numbers come from the counter-based Philox4x64-10
+ * generator (Salmon, Moraes, Dror, Shaw, SC'11): key = {seed, stream}, counter =
+ * {body index, block, 0, 0}, so every body draws independently of the others and the
+ * result does not depend on the launch shape.  A uniform double is
+ * (word >> 11) * 2^-53, as numpy's generators convert 64-bit words.
+ *
+ *  UNIFORM_CUBE  r ~ U[-half, half]^3, v ~ N(0, v_sigma^2)^3 (Box-Muller),
+ *                m ~ U[m_lo, m_hi]: the bench configurations' bodies.
+ *  PLUMMER       one Plummer sphere of scale radius a (Aarseth, Henon & Wielen 1974:
+ *                radius from the inverted cumulative mass cut at 99.9 %, isotropic
+ *                directions, speed q * v_esc with q drawn by rejection from
+ *                q^2 (1 - q^2)^(7/2)), masses log-uniform in [m_lo, m_hi], then shifted
+ *                so that its centre of mass sits at (cx, cy, cz) moving with
+ *                (cvx, cvy, cvz).  Two calls with different streams and offsets into
+ *                r/v make the colliding pair.
+ *  GALAXY        the reference's galaxy recipe (simulation.py:99-184): a central mass
+ *                m_hole at the origin and n - 1 stars of m_star on circular orbits about
+ *                it, the first 4/5 in a thin disc, the rest in a bulge; SI inputs are
+ *                scaled by scale_r / scale_m as add_object does (_base_.py:114-117) and
+ *                G is the universe's scaled G (_base_.py:85-88), used for the orbital
+ *                speeds as the recipe does (simulation.py:147-149).
+ *
+ * Output: r (x, y, z, G*m) and v (vx, vy, vz, 0), n rows of 4 doubles each, the packed
+ * layout of grav_batch (pass r + 4 * body_off for a universe inside a batch).
+ */
+typedef struct grav_scenario {
+	int32_t kind;
+	int32_t _pad0;
+	uint64_t seed;
+	uint64_t stream;
+	double G;     /* column 3 of r receives G * m */
+	double p[10]; /* kind parameters, see GRAV_SCEN_* */
+} grav_scenario;
+
+/* Device scratch grav_scenario_generate needs for n bodies of this kind (0: none). */
+int64_t grav_scenario_scratch_bytes(const grav_scenario* s, int64_t n);
+
+/*
+ * Writes n bodies of scenario s into the device (or device-addressable) arrays r and v
+ * (32-byte aligned).  scratch: grav_scenario_scratch_bytes() bytes of device memory
+ * (NULL when that is 0).  Deterministic: the same s and n give the same bits on every
+ * call.  Replaces the reference's Python generators + add_object loop
+ * (simulation.py:85-184, _base_.py:107-118) for the bodies' initial state.
+ */
+int grav_scenario_generate(const grav_scenario* s, double* r, double* v, int64_t n,
+	void* scratch, void* stream);
+
 /* ---- host-resident state ------------------------------------------------------------ */
 
 /*

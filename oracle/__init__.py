@@ -60,8 +60,44 @@ def lib():
         L.orc_vjp_fp64.argtypes = [_dp, _dp, ctypes.c_double, _dp, ctypes.c_int64,
                                    _dp, _dp, ctypes.c_int]
         L.orc_vjp_fp64.restype = None
+        _u64p = ctypes.POINTER(ctypes.c_uint64)
+        L.orc_philox4x64_10.argtypes = [_u64p, _u64p, _u64p]
+        L.orc_philox4x64_10.restype = None
+        L.orc_scenario.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64,
+                                   ctypes.c_double, _dp, ctypes.c_int64, _dp, _dp]
+        L.orc_scenario.restype = ctypes.c_int
         _LIB = L
     return _LIB
+
+
+# ---------------------------------------------------------------------------------
+# seeded scenarios (restatement of the device generator, oracle/scenario.c)
+# ---------------------------------------------------------------------------------
+
+SCENARIO_KINDS = {'uniform_cube': 1, 'plummer': 2, 'galaxy': 3}
+
+
+def philox4x64_10(ctr, key):
+    """Philox4x64-10 block for a 4-word counter and a 2-word key (uint64 array [4])."""
+    c = np.ascontiguousarray(ctr, dtype=np.uint64)
+    k = np.ascontiguousarray(key, dtype=np.uint64)
+    out = np.zeros(4, dtype=np.uint64)
+    u64 = ctypes.POINTER(ctypes.c_uint64)
+    lib().orc_philox4x64_10(_ptr(c, u64), _ptr(k, u64), _ptr(out, u64))
+    return out
+
+
+def scenario(kind, n, seed, stream, G, params):
+    """(r, v): n x 4 float64 arrays (x, y, z, G*m) / (vx, vy, vz, 0) of a scenario."""
+    p = np.zeros(10)
+    p[:len(params)] = params
+    r = np.zeros((n, 4))
+    v = np.zeros((n, 4))
+    k = SCENARIO_KINDS[kind] if isinstance(kind, str) else int(kind)
+    if lib().orc_scenario(k, int(seed), int(stream), float(G), _ptr(p, _dp), int(n),
+                          _ptr(r, _dp), _ptr(v, _dp)) != 0:
+        raise ValueError('unknown scenario kind %r' % (kind,))
+    return r, v
 
 
 def port_lib():

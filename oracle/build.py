@@ -1,7 +1,8 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
 Builds, with gcc, next to this file:
-  liboracle.so  -- oracle.c: FP64 all-pairs oracle, FP64 stage 2, energy, adjoint check
+  liboracle.so  -- oracle.c: FP64 all-pairs oracle, FP64 stage 2, energy, adjoint check;
+                   scenario.c: the seeded scenario generator restated
   libport.so    -- ref_port.c: portable restatement of the reference's fastest CPU
                    stage 1 (the timed CPU baseline)
 and, only where the reference tree is present (this is never the case on the GPU
@@ -41,10 +42,10 @@ def _newer(target, *sources):
 
 def build_oracle(force=False):
     out = os.path.join(HERE, 'liboracle.so')
-    src = os.path.join(HERE, 'oracle.c')
-    if force or not _newer(out, src):
+    srcs = [os.path.join(HERE, 'oracle.c'), os.path.join(HERE, 'scenario.c')]
+    if force or not _newer(out, *srcs):
         _run(['gcc', '-O2', '-fPIC', '-shared', '-fopenmp', '-ffp-contract=off',
-              '-std=gnu11', '-Wall', src, '-o', out, '-lm'])
+              '-std=gnu11', '-Wall'] + srcs + ['-o', out, '-lm'])
     return out
 
 

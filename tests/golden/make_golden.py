@@ -12,6 +12,8 @@ gravitation/kernel/), on seeded inputs:
   py1 FP64  N=128, seed 0, 5 steps    -> accelerations of step 0, final state
   galaxy    N=256 (seeded galaxy recipe, the reference's galaxy parameters, np1 FP32),
             2 steps -> accelerations of step 0
+  galdev    N=300: the reference's own create_galaxy driven by the device scenario
+            generator's Philox draws (pins the galaxy part of the scenario generator)
 Inputs follow the uniform-cube workload: r ~ U[-1000,1000]^3, v ~ N(0,1), m ~ U[1,100]
 (numpy default_rng(seed)), G, T and scaling at universe_base defaults.
 
@@ -97,9 +99,48 @@ def main():
     out['gal_scale_m'] = np.float64(gpar['scale_m'])
     out['gal_scale_r'] = np.float64(gpar['scale_r'])
 
+    out.update(reference_galaxy(args.ref, n=300, seed=5, stream=0))
+
     path = os.path.join(HERE, 'golden_ref.npz')
     np.savez_compressed(path, **out)
     print('wrote', path, os.path.getsize(path), 'bytes')
+
+
+def reference_galaxy(ref, n, seed, stream):
+    """The reference's own create_galaxy (gravitation/lib/simulation.py:99-184, with the
+    galaxy scenario's arguments, simulation.py:57-77) fed with the draws of the seeded
+    device generator: for the call, random.random returns words 0, 1, 2 of Philox4x64-10
+    block {body, 0} under key {seed, stream} for body 1, 2, ..., n-1 in turn (the
+    uniforms the generator gives star k = body k+1).  The bodies land, scaled by
+    add_object, in a reference universe_base.  simulation.py imports h5py at module
+    level; the galaxy code does not use it, so a stand-in module satisfies the import."""
+    import importlib
+    import types
+    sys.modules.setdefault('h5py', types.ModuleType('h5py'))
+    sim = importlib.import_module('gravitation.lib.simulation')
+    base = importlib.import_module('gravitation.kernel._base_')
+    import oracle
+    draws = []
+    for i in range(1, n):
+        w = oracle.philox4x64_10([i, 0, 0, 0], [seed, stream])
+        draws += [float(int(x) >> 11) * 2.0 ** -53 for x in w[:3]]
+    it = iter(draws)
+    saved = sim.random.random
+    sim.random.random = lambda: next(it)
+    try:
+        u = base.universe_base(T=2.0e12, scale_m=1.0e-30, scale_r=1.0e-10, dtype='float32')
+        sim.create_galaxy(universe_obj=u, stars_len=n - 1, r=[0., 0., 0.], v=[0., 0., 0.],
+                          g_alpha=0., g_beta=0., m_hole=4e40, m_star=2e30, radius=1e20)
+    finally:
+        sim.random.random = saved
+    assert next(it, None) is None, 'create_galaxy drew a different number of uniforms'
+    return {
+        'galdev_r': np.array([[float(c) for c in pm._r] for pm in u._mass_list]),
+        'galdev_v': np.array([[float(c) for c in pm._v] for pm in u._mass_list]),
+        'galdev_m': np.array([float(pm._m) for pm in u._mass_list]),
+        'galdev_G': np.float64(u._G),
+        'galdev_seed': np.int64(seed), 'galdev_stream': np.int64(stream),
+    }
 
 
 if __name__ == '__main__':
