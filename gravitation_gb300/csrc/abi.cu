@@ -363,8 +363,10 @@ int grav_stage1(const grav_batch* b, void* stream)
 			b->tile.bpt, b->tile.threads, b->tile.jtile, b->mode);
 	grav_batch copy = *b;
 	void* args[] = {&copy};
-	cudaError_t e = cudaLaunchKernel(k->fn, dim3(b->tile.grid), dim3(b->tile.threads), args,
-		k->smem_bytes, static_cast<cudaStream_t>(stream));
+	cudaStream_t st = static_cast<cudaStream_t>(stream);
+	cudaError_t e = k->dependent
+		? grav::launch_dependent(k->fn, b->tile.grid, b->tile.threads, k->smem_bytes, st, args)
+		: cudaLaunchKernel(k->fn, dim3(b->tile.grid), dim3(b->tile.threads), args, k->smem_bytes, st);
 	if (e != cudaSuccess) return cuda_fail(e, "stage-1 kernel launch");
 	return ok();
 }

@@ -170,6 +170,8 @@ __global__ void __launch_bounds__(256) adjoint_stage2_kernel(const grav_batch b,
 	const grav_seg_desc S = b.seg[seg];
 	const grav_univ_desc U = b.univ[S.u];
 	const int il = S.il0 + li;
+	// slots, state, gradients and positions belong to the kernels before this one
+	grid_dep_wait();
 	float4* pos = static_cast<float4*>(b.pos);
 	if (il >= U.n) {
 		pos[g] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -185,11 +187,25 @@ __global__ void __launch_bounds__(256) adjoint_stage2_kernel(const grav_batch b,
 	arow4 r = rr[row], v = vv[row], a_gr = grr[row], a_gv = gvv[row];
 
 	if (flags & ADJ_STEP) {
+		// slots added in slot order, their loads issued SLOT_BATCH slots at a time
+		constexpr int SLOT_BATCH = 4;
 		double s[7] = {0, 0, 0, 0, 0, 0, 0};
-		for (int k = 0; k < S.nslots; ++k) {
-			const double* p = b.part + static_cast<int64_t>(S.slot_base + k) * 7 * IT + li;
+		const double* part = b.part + static_cast<int64_t>(S.slot_base) * 7 * IT + li;
+		int k = 0;
+		for (; k + SLOT_BATCH <= S.nslots; k += SLOT_BATCH) {
+			double q[SLOT_BATCH][7];
 #pragma unroll
-			for (int c = 0; c < 7; ++c) s[c] += p[c * IT];
+			for (int j = 0; j < SLOT_BATCH; ++j)
+#pragma unroll
+				for (int c = 0; c < 7; ++c) q[j][c] = __ldg(part + (static_cast<int64_t>(k + j) * 7 + c) * IT);
+#pragma unroll
+			for (int j = 0; j < SLOT_BATCH; ++j)
+#pragma unroll
+				for (int c = 0; c < 7; ++c) s[c] += q[j][c];
+		}
+		for (; k < S.nslots; ++k) {
+#pragma unroll
+			for (int c = 0; c < 7; ++c) s[c] += __ldg(part + (static_cast<int64_t>(k) * 7 + c) * IT);
 		}
 		// reverse the forward update: r_k = r_{k+1} - T v_{k+1}; v_k = v_{k+1} - T a_k
 		r.x = __dsub_rn(r.x, __dmul_rn(v.x, T));
@@ -222,6 +238,23 @@ __global__ void __launch_bounds__(256) adjoint_stage2_kernel(const grav_batch b,
 		upos[g] = make_float4(__double2float_rn(a_gv.x + T * a_gr.x),
 			__double2float_rn(a_gv.y + T * a_gr.y), __double2float_rn(a_gv.z + T * a_gr.z), 0.f);
 	}
+}
+
+// Adjoint stage 2 as a programmatic dependent of the kernel before it (it waits with
+// grid_dep_wait); small CTAs so that a few thousand rows still spread over many SMs.
+cudaError_t launch_adjoint_stage2(const grav_batch& b, const grav_adjoint& a, int flags,
+	cudaStream_t st)
+{
+	grav_batch copy = b;
+	double* gr = static_cast<double*>(a.gr);
+	double* gv = static_cast<double*>(a.gv);
+	double* ggm = static_cast<double*>(a.ggm);
+	float4* upos = static_cast<float4*>(a.upos);
+	int f = flags;
+	void* args[] = {&copy, &gr, &gv, &ggm, &upos, &f};
+	const unsigned blocks = static_cast<unsigned>((b.n_pad_total + 63) / 64);
+	return launch_dependent(reinterpret_cast<const void*>(&adjoint_stage2_kernel), blocks, 64, 0,
+		st, args);
 }
 
 struct VjpKernel {
@@ -305,10 +338,7 @@ extern "C" int grav_adjoint_prepare(const grav_adjoint* a, void* stream)
 	if (b.n_pad_total == 0) return GRAV_OK;
 	grav_batch copy = b;
 	copy.part = a->part7;
-	const unsigned blocks = static_cast<unsigned>((b.n_pad_total + 255) / 256);
-	grav::adjoint_stage2_kernel<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
-		copy, a->gr, a->gv, a->ggm, static_cast<float4*>(a->upos), ADJ_PREPARE);
-	cudaError_t e = cudaGetLastError();
+	cudaError_t e = grav::launch_adjoint_stage2(copy, *a, ADJ_PREPARE, static_cast<cudaStream_t>(stream));
 	return e == cudaSuccess ? GRAV_OK : grav::record_error(GRAV_E_CUDA, cudaGetErrorString(e));
 }
 
@@ -334,12 +364,9 @@ extern "C" int grav_adjoint_step(const grav_adjoint* a, void* stream)
 		if (!k) return grav::record_error(GRAV_E_TILE, "tile shape has no adjoint kernel");
 		const float4* up = static_cast<const float4*>(a->upos);
 		void* args[] = {&copy, &up};
-		cudaError_t e = cudaLaunchKernel(k->fn, dim3(b.tile.grid), dim3(k->threads), args, k->smem, st);
+		cudaError_t e = grav::launch_dependent(k->fn, b.tile.grid, k->threads, k->smem, st, args);
 		if (e != cudaSuccess) return grav::record_error(GRAV_E_CUDA, cudaGetErrorString(e));
 	}
-	const unsigned blocks = static_cast<unsigned>((b.n_pad_total + 255) / 256);
-	grav::adjoint_stage2_kernel<<<blocks, 256, 0, st>>>(copy, a->gr, a->gv, a->ggm,
-		static_cast<float4*>(a->upos), ADJ_STEP | ADJ_PREPARE);
-	cudaError_t e = cudaGetLastError();
+	cudaError_t e = grav::launch_adjoint_stage2(copy, *a, ADJ_STEP | ADJ_PREPARE, st);
 	return e == cudaSuccess ? GRAV_OK : grav::record_error(GRAV_E_CUDA, cudaGetErrorString(e));
 }

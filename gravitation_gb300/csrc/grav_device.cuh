@@ -109,10 +109,52 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x)
 	lo += e;
 }
 
+// Programmatic dependent launch.  A kernel launched with programmatic stream
+// serialization may start while the kernel before it in the stream is still running:
+// grid_dep_wait() blocks until that kernel has completed and its memory operations are
+// visible, so everything before it may only read data no earlier kernel writes (plan
+// tables, launch arguments).  grid_dep_launch() lets the next kernel in the stream
+// start its own launch.  Both are no-ops for a kernel launched the ordinary way.
+__device__ __forceinline__ void grid_dep_wait()
+{
+	asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+__device__ __forceinline__ void grid_dep_launch()
+{
+	asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // Record the first error code seen by any CTA.
 __device__ __forceinline__ void set_error(int* err, int code)
 {
 	if (err) atomicCAS(err, 0, code);
+}
+
+// Index of the last plan segment whose unit_begin <= ub (unit_begin never decreases
+// along the table and seg[0].unit_begin = 0 <= ub).  Each warp searches on its own:
+// per round its 32 lanes probe 32 evenly spaced candidates and a ballot keeps the
+// interval between the last candidate that qualifies and the next one, so the search
+// takes ceil(log32(n_seg)) rounds of independent loads where a bisection takes
+// log2(n_seg) dependent ones.  All 32 lanes of the warp must call it together.
+__device__ __forceinline__ int find_segment(const grav_seg_desc* seg, int n_seg, int64_t ub)
+{
+	const unsigned full = 0xffffffffu;
+	const int lane = threadIdx.x & 31;
+	int lo = 0, hi = n_seg - 1;
+	while (lo < hi) {
+		const int span = hi - lo + 1;  // candidates left, >= 2
+		const int idx = span <= 32 ? lo + min(lane, span - 1)
+		                           : lo + static_cast<int>((static_cast<int64_t>(lane) * span) / 32);
+		const unsigned ok = __ballot_sync(full, seg[idx].unit_begin <= ub);  // lane 0 qualifies
+		const int top = 31 - __clz(ok);
+		const int at = __shfl_sync(full, idx, top);
+		const int after = __shfl_sync(full, idx, (top + 1) & 31);
+		if (span <= 32) return at;
+		hi = top < 31 ? after - 1 : hi;
+		lo = at;
+	}
+	return lo;
 }
 
 }  // namespace grav

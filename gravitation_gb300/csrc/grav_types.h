@@ -1,6 +1,8 @@
 // grav_types.h -- internal constants shared by host and device code of libgravgb300.
 #pragma once
 
+#include <cuda_runtime.h>
+
 #include "gravitation_gb300.h"
 
 // Wall-clock bound of every device-side wait on a bulk copy (nanoseconds).
@@ -13,11 +15,31 @@ struct Stage1Kernel {
 	int mode, bpt, threads, jtile;
 	const void* fn;       // __global__ function
 	int smem_bytes;       // dynamic shared memory per CTA
+	bool dependent;       // waits with grid_dep_wait(): may launch as a programmatic dependent
 };
 
 // Kernel tables, one per translation unit (stage1_f32.cu, stage1_f64.cu).
 int stage1_table_f32(const Stage1Kernel** out);
 int stage1_table_f64(const Stage1Kernel** out);
 int stage1_table_sym(const Stage1Kernel** out);
+
+// Launch with programmatic stream serialization: the kernel may begin while the kernel
+// before it in the stream finishes; it must call grid_dep_wait() (grav_device.cuh)
+// before touching anything that kernel, or one before it, writes.
+inline cudaError_t launch_dependent(const void* fn, unsigned grid, unsigned threads,
+	size_t smem, cudaStream_t stream, void** args)
+{
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = dim3(grid);
+	cfg.blockDim = dim3(threads);
+	cfg.dynamicSmemBytes = smem;
+	cfg.stream = stream;
+	cudaLaunchAttribute attr[1];
+	attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	attr[0].val.programmaticStreamSerializationAllowed = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	return cudaLaunchKernelExC(&cfg, fn, args);
+}
 
 }  // namespace grav

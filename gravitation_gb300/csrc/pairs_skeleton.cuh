@@ -51,16 +51,9 @@ __device__ __forceinline__ void run_pairs(const grav_batch& b, Op& op)
 	}
 	__syncthreads();
 
-	int s;
-	{
-		int lo = 0, hi = b.n_seg - 1;
-		while (lo < hi) {
-			const int mid = (lo + hi + 1) >> 1;
-			if (b.seg[mid].unit_begin <= ub) lo = mid;
-			else hi = mid - 1;
-		}
-		s = lo;
-	}
+	int s = find_segment(b.seg, b.n_seg, ub);
+	// positions, u and slots belong to the kernels before this one
+	grid_dep_wait();
 
 	uint32_t gt = 0;
 	bool timed_out = false;
@@ -114,6 +107,8 @@ __device__ __forceinline__ void run_pairs(const grav_batch& b, Op& op)
 		++s;
 	}
 
+	// the next kernel in the stream may start launching now (it waits for this grid)
+	grid_dep_launch();
 	if (timed_out && tid == 0) {
 		set_error(b.err, GRAV_DEV_TIMEOUT);
 		mbar_wait_bounded(&bar[gt & 1], (gt >> 1) & 1);

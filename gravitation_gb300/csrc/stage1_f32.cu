@@ -56,16 +56,9 @@ __global__ void __launch_bounds__(T) stage1_f32_kernel(const grav_batch b)
 	const float eps2 = b.eps2;
 
 	// segment holding unit ub: the last segment whose unit_begin <= ub
-	int s;
-	{
-		int lo = 0, hi = b.n_seg - 1;
-		while (lo < hi) {
-			const int mid = (lo + hi + 1) >> 1;
-			if (b.seg[mid].unit_begin <= ub) lo = mid;
-			else hi = mid - 1;
-		}
-		s = lo;
-	}
+	int s = find_segment(b.seg, b.n_seg, ub);
+	// positions and partial-sum slots belong to the kernels before this one
+	grid_dep_wait();
 
 	uint32_t gt = 0;  // tiles consumed by this CTA so far (buffer gt&1, parity (gt>>1)&1)
 	bool timed_out = false;
@@ -181,6 +174,9 @@ __global__ void __launch_bounds__(T) stage1_f32_kernel(const grav_batch b)
 		++s;
 	}
 
+	// the next kernel in the stream may start launching now (it waits for this grid);
+	// not earlier, so that its CTAs find the SMs this persistent grid leaves
+	grid_dep_launch();
 	if (timed_out && tid == 0) {
 		set_error(b.err, GRAV_DEV_TIMEOUT);
 		// the copy that did not arrive is the only one in flight; give it one more
@@ -191,7 +187,7 @@ __global__ void __launch_bounds__(T) stage1_f32_kernel(const grav_batch b)
 
 #define GRAV_F32_ENTRY(MODE, B, T, J) \
 	{MODE, B, T, J, reinterpret_cast<const void*>(&stage1_f32_kernel<MODE, B, T, J>), \
-		2 * ((MODE == GRAV_MODE_FP32C) ? 2 : 1) * J * 16}
+		2 * ((MODE == GRAV_MODE_FP32C) ? 2 : 1) * J * 16, true}
 
 static const Stage1Kernel k_table_f32[] = {
 	GRAV_F32_ENTRY(GRAV_MODE_FP32, 1, 128, 128),

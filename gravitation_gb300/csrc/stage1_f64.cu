@@ -39,16 +39,9 @@ __global__ void __launch_bounds__(T) stage1_f64_kernel(const grav_batch b)
 
 	const dpos4* __restrict__ pos = static_cast<const dpos4*>(b.pos);
 
-	int s;
-	{
-		int lo = 0, hi = b.n_seg - 1;
-		while (lo < hi) {
-			const int mid = (lo + hi + 1) >> 1;
-			if (b.seg[mid].unit_begin <= ub) lo = mid;
-			else hi = mid - 1;
-		}
-		s = lo;
-	}
+	int s = find_segment(b.seg, b.n_seg, ub);
+	// positions and partial-sum slots belong to the kernels before this one
+	grid_dep_wait();
 
 	uint32_t gt = 0;
 	bool timed_out = false;
@@ -126,6 +119,8 @@ __global__ void __launch_bounds__(T) stage1_f64_kernel(const grav_batch b)
 		++s;
 	}
 
+	// the next kernel in the stream may start launching now (it waits for this grid)
+	grid_dep_launch();
 	if (timed_out && tid == 0) {
 		set_error(b.err, GRAV_DEV_TIMEOUT);
 		mbar_wait_bounded(&bar[gt & 1], (gt >> 1) & 1);
@@ -134,7 +129,7 @@ __global__ void __launch_bounds__(T) stage1_f64_kernel(const grav_batch b)
 
 #define GRAV_F64_ENTRY(B, T, J) \
 	{GRAV_MODE_FP64, B, T, J, reinterpret_cast<const void*>(&stage1_f64_kernel<B, T, J>), \
-		2 * J * 32}
+		2 * J * 32, true}
 
 static const Stage1Kernel k_table_f64[] = {
 	GRAV_F64_ENTRY(1, 128, 128),

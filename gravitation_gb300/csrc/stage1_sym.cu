@@ -64,6 +64,10 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 	const float4* __restrict__ pos = static_cast<const float4*>(b.pos);
 	const float eps2 = b.eps2;
 
+	// Segment of unit ub by bisection, and no programmatic-launch instructions: this
+	// kernel runs for 1e5-1e6 cycles per CTA, where a few microseconds of prologue do
+	// not matter, and with the warp-parallel search or griddepcontrol in it the
+	// compiled main loop measured 1-4 % slower on GB300 (N = 65536, tile 8/128/256).
 	int s;
 	{
 		int lo = 0, hi = b.n_seg - 1;
@@ -252,12 +256,13 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 	}
 }
 
+// launched the ordinary way (not as a programmatic dependent): see the kernel's prologue
 #define GRAV_SYM_ENTRY(B, W, J) \
 	{GRAV_MODE_FP32U, B, 32 * W, J, \
-		reinterpret_cast<const void*>(&stage1_sym_kernel<B, W, J, 4, 1>), 2 * J * 16}
+		reinterpret_cast<const void*>(&stage1_sym_kernel<B, W, J, 4, 1>), 2 * J * 16, false}
 #define GRAV_SYMC_ENTRY(B, W, J) \
 	{GRAV_MODE_FP32CU, B, 32 * W, J, \
-		reinterpret_cast<const void*>(&stage1_sym_kernel<B, W, J, 4, 2>), 2 * 2 * J * 16}
+		reinterpret_cast<const void*>(&stage1_sym_kernel<B, W, J, 4, 2>), 2 * 2 * J * 16, false}
 
 static const Stage1Kernel k_table_sym[] = {
 	GRAV_SYM_ENTRY(4, 4, 128),

@@ -17,6 +17,9 @@ struct __align__(32) drow4 {
 
 __global__ void __launch_bounds__(256) stage2_kernel(const grav_batch b, const int flags)
 {
+	// launched as a dependent of stage 1; the next stage 1 may start launching when
+	// this grid's CTAs exit (no earlier trigger: the persistent stage-1 grid should
+	// find its SMs free)
 	const int64_t g = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
 	if (g >= b.n_pad_total) return;
 	const int IT = b.tile.bpt * b.tile.threads;
@@ -25,6 +28,8 @@ __global__ void __launch_bounds__(256) stage2_kernel(const grav_batch b, const i
 	const grav_seg_desc S = b.seg[seg];
 	const grav_univ_desc U = b.univ[S.u];
 	const int il = S.il0 + li;
+	// slots, positions and the state belong to the kernels before this one
+	grid_dep_wait();
 
 	if (il >= U.n) {
 		if (b.mode == GRAV_MODE_FP64) {
@@ -43,13 +48,34 @@ __global__ void __launch_bounds__(256) stage2_kernel(const grav_batch b, const i
 	drow4 r = rr[row];
 
 	if (!(flags & GRAV_S2_PREPARE)) {
+		// slots are added in slot order; their loads are issued SLOT_BATCH at a time so
+		// that a long slot list costs a few memory latencies, not one per slot
+		constexpr int SLOT_BATCH = 8;
 		double ax = 0.0, ay = 0.0, az = 0.0;
-		const double* __restrict__ part = b.part;
-		for (int k = 0; k < S.nslots; ++k) {
-			const int64_t base = static_cast<int64_t>(S.slot_base + k) * 3 * IT + li;
-			ax += part[base];
-			ay += part[base + IT];
-			az += part[base + 2 * IT];
+		const double* __restrict__ part = b.part + static_cast<int64_t>(S.slot_base) * 3 * IT + li;
+		const int64_t stride = 3 * static_cast<int64_t>(IT);
+		int k = 0;
+		for (; k + SLOT_BATCH <= S.nslots; k += SLOT_BATCH) {
+			double px[SLOT_BATCH], py[SLOT_BATCH], pz[SLOT_BATCH];
+#pragma unroll
+			for (int q = 0; q < SLOT_BATCH; ++q) {
+				const double* p = part + (k + q) * stride;
+				px[q] = __ldg(p);
+				py[q] = __ldg(p + IT);
+				pz[q] = __ldg(p + 2 * IT);
+			}
+#pragma unroll
+			for (int q = 0; q < SLOT_BATCH; ++q) {
+				ax += px[q];
+				ay += py[q];
+				az += pz[q];
+			}
+		}
+		for (; k < S.nslots; ++k) {
+			const double* p = part + k * stride;
+			ax += __ldg(p);
+			ay += __ldg(p + IT);
+			az += __ldg(p + 2 * IT);
 		}
 		if ((flags & GRAV_S2_WRITE_A) && b.a_out)
 			reinterpret_cast<drow4*>(b.a_out)[row] = drow4{ax, ay, az, 0.0};
@@ -88,10 +114,14 @@ __global__ void __launch_bounds__(256) stage2_kernel(const grav_batch b, const i
 cudaError_t launch_stage2(const grav_batch& b, int flags, cudaStream_t stream)
 {
 	if (b.n_pad_total == 0) return cudaSuccess;
-	const int threads = 256;
+	// small CTAs: a few thousand rows still spread over many SMs (latency bound)
+	const int threads = 64;
 	const int64_t blocks = (b.n_pad_total + threads - 1) / threads;
-	stage2_kernel<<<static_cast<unsigned>(blocks), threads, 0, stream>>>(b, flags);
-	return cudaGetLastError();
+	grav_batch copy = b;
+	int f = flags;
+	void* args[] = {&copy, &f};
+	return launch_dependent(reinterpret_cast<const void*>(&stage2_kernel),
+		static_cast<unsigned>(blocks), threads, 0, stream, args);
 }
 
 }  // namespace grav
