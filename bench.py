@@ -62,7 +62,8 @@ def parse():
     ap.add_argument('--no-batched', action='store_true')
     ap.add_argument('--no-adjoint', action='store_true')
     ap.add_argument('--workload', default=None,
-                    choices=('precision', 'sweep', 'adjoint', 'adjoint-check', 'scenario'),
+                    choices=('precision', 'sweep', 'adjoint', 'adjoint-check', 'scenario',
+                             'frontend'),
                     help='run one secondary workload instead of the headline step')
     ap.add_argument('--profile', action='store_true',
                     help='only set up the workload and run --steps stage-1 launches '
@@ -504,6 +505,8 @@ def run_workload(args):
         res = workloads.run_adjoint_check()
     elif args.workload == 'scenario':
         res = workloads.run_generate(hbm_gbs=measured_peaks().get('hbm_gbs'))
+    elif args.workload == 'frontend':
+        res = workloads.run_frontend()
     else:
         raise SystemExit('unknown workload %r' % args.workload)
     res['workload_name'] = args.workload

@@ -17,11 +17,12 @@
 // s while the chunk's column sums rotate one lane per step (shfl), so after 32 steps
 // every row of the warp has met every body of the chunk once and each lane holds the
 // complete column sum of "its" body.  Warps add their column sums into shared memory
-// (atomics), and the tile's column sums go, as FP64, into the column slot of (I, J):
-// block J's segment lists its row slots first and then one column slot per block
-// I < J, so stage 2 adds them like any partial sums (fixed order, deterministic).
+// (atomics), and the tile's column sums go into the column slot of (I, J): block J's
+// segment lists its row slots first and then one column slot per block I < J (its last
+// J slots), so stage 2 adds them like any partial sums (fixed order, deterministic).
 // Row sums are FP32 per tile, folded into compensated (TwoSum) FP32 hi+lo sums, as in
-// stage1_f32.cu; column sums are FP32 per tile and go out as FP64.
+// stage1_f32.cu, and go out as FP64; column sums are FP32 per tile and go out as FP32
+// (the first 3R floats of the slot), which stage 2 widens exactly.
 #include "grav_device.cuh"
 
 namespace grav {
@@ -215,15 +216,18 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 					atomicAdd(&colacc[2][ch * 32 + lane], cz);
 				}
 				__syncthreads();
-				// column sums of this tile -> column slot of (I, J), then clear
+				// column sums of this tile -> column slot of (I, J), then clear.  They are
+				// FP32 sums, so they go out as FP32 (first half of the slot; stage 2
+				// widens them exactly): half the bytes of an FP64 slot
 				const int sJ = s + (blkJ - blkI);
 				const grav_seg_desc SJ = b.seg[sJ];
 				const int64_t slot = SJ.slot_base + SJ.nslots - (blkJ - blkI);
-				double* __restrict__ out = b.part + slot * 3 * R + (jt * JT - static_cast<int64_t>(blkJ) * R);
+				float* __restrict__ out = reinterpret_cast<float*>(b.part + slot * 3 * R) +
+					(jt * JT - static_cast<int64_t>(blkJ) * R);
 				for (int i = tid; i < JT; i += T) {
-					out[i] = static_cast<double>(colacc[0][i]);
-					out[R + i] = static_cast<double>(colacc[1][i]);
-					out[2 * R + i] = static_cast<double>(colacc[2][i]);
+					out[i] = colacc[0][i];
+					out[R + i] = colacc[1][i];
+					out[2 * R + i] = colacc[2][i];
 					colacc[0][i] = colacc[1][i] = colacc[2][i] = 0.f;
 				}
 			}

@@ -54,8 +54,12 @@ __global__ void __launch_bounds__(256) stage2_kernel(const grav_batch b, const i
 		double ax = 0.0, ay = 0.0, az = 0.0;
 		const double* __restrict__ part = b.part + static_cast<int64_t>(S.slot_base) * 3 * IT + li;
 		const int64_t stride = 3 * static_cast<int64_t>(IT);
+		// unique-pair plans: the last (row block index) slots of a segment are column
+		// slots holding FP32 sums in their first half (stage1_sym.cu)
+		const bool pairs = b.mode == GRAV_MODE_FP32U || b.mode == GRAV_MODE_FP32CU;
+		const int nrow = pairs ? S.nslots - S.il0 / IT : S.nslots;
 		int k = 0;
-		for (; k + SLOT_BATCH <= S.nslots; k += SLOT_BATCH) {
+		for (; k + SLOT_BATCH <= nrow; k += SLOT_BATCH) {
 			double px[SLOT_BATCH], py[SLOT_BATCH], pz[SLOT_BATCH];
 #pragma unroll
 			for (int q = 0; q < SLOT_BATCH; ++q) {
@@ -71,11 +75,36 @@ __global__ void __launch_bounds__(256) stage2_kernel(const grav_batch b, const i
 				az += pz[q];
 			}
 		}
-		for (; k < S.nslots; ++k) {
+		for (; k < nrow; ++k) {
 			const double* p = part + k * stride;
 			ax += __ldg(p);
 			ay += __ldg(p + IT);
 			az += __ldg(p + 2 * IT);
+		}
+		const float* __restrict__ cpart =
+			reinterpret_cast<const float*>(b.part + static_cast<int64_t>(S.slot_base) * 3 * IT) + li;
+		const int64_t fstride = 2 * stride;  // floats per slot
+		for (; k + SLOT_BATCH <= S.nslots; k += SLOT_BATCH) {
+			float px[SLOT_BATCH], py[SLOT_BATCH], pz[SLOT_BATCH];
+#pragma unroll
+			for (int q = 0; q < SLOT_BATCH; ++q) {
+				const float* p = cpart + (k + q) * fstride;
+				px[q] = __ldg(p);
+				py[q] = __ldg(p + IT);
+				pz[q] = __ldg(p + 2 * IT);
+			}
+#pragma unroll
+			for (int q = 0; q < SLOT_BATCH; ++q) {
+				ax += static_cast<double>(px[q]);
+				ay += static_cast<double>(py[q]);
+				az += static_cast<double>(pz[q]);
+			}
+		}
+		for (; k < S.nslots; ++k) {
+			const float* p = cpart + k * fstride;
+			ax += static_cast<double>(__ldg(p));
+			ay += static_cast<double>(__ldg(p + IT));
+			az += static_cast<double>(__ldg(p + 2 * IT));
 		}
 		if ((flags & GRAV_S2_WRITE_A) && b.a_out)
 			reinterpret_cast<drow4*>(b.a_out)[row] = drow4{ax, ay, az, 0.0};

@@ -142,8 +142,10 @@ class GB300Stages:
         self._gb_ha = torch.zeros((n, 4), dtype=torch.float64, pin_memory=pin)
         hr, hv, ha = self._gb_hr.numpy(), self._gb_hv.numpy(), self._gb_ha.numpy()
         self._gb_herr = torch.zeros(1, dtype=torch.int32, pin_memory=pin)
+        self._gb_herr_np = self._gb_herr.numpy()
         self._gb_stream = torch.cuda.Stream(device=dev)
         self._gb_side = torch.cuda.Stream(device=dev)
+        self._gb_wait = self._gb_stream  # the stream the queued step runs on
         if parts is not None:
             # bodies written by the device, then one copy into the host mirror
             self._gb.generate_state([parts], G=self._G, stream=self._gb_stream)
@@ -233,9 +235,9 @@ class GB300Stages:
 
     def _gb_finish(self):
         """Wait for the queued work; raise on the device error flag it copied back."""
-        self._gb_stream.synchronize()
-        code = int(self._gb_herr[0])
-        if code != _lib.GRAV_DEV_OK:
+        self._gb_wait.synchronize()
+        self._gb_wait = self._gb_stream
+        if int(self._gb_herr_np[0]) != _lib.GRAV_DEV_OK:
             self._gb.raise_on_device_error()
 
     def _gb_download(self, state=True):
@@ -245,10 +247,15 @@ class GB300Stages:
     def step_stage1(self):
         if self._gb_fuse:
             if self._gb_graph is not None:
-                # replay() launches on the current stream: make it the kernel's stream,
-                # the one _gb_finish waits for
-                with torch.cuda.stream(self._gb_stream):
+                # replay() launches on the current stream; the step is synchronous, so
+                # step_stage2 waits for that stream (entering a stream context for the
+                # replay would cost more than the replay's own launch)
+                if torch.cuda.current_device() == self._gb.device.index:
+                    self._gb_wait = torch.cuda.current_stream()
                     self._gb_graph.replay()
+                else:
+                    with torch.cuda.stream(self._gb_stream):
+                        self._gb_graph.replay()
             else:
                 self._gb_enqueue_step()
             return

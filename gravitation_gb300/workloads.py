@@ -4,6 +4,12 @@
                 per stage, the steady-state step replayed from a CUDA graph, tile shape
                 from the autotuner -- against looping the single-universe step over the
                 universes (one Engine per universe, each with its own tuned tile)
+  run_adjoint   forward rollout vs forward + adjoint (N = 4096, 1000 steps)
+  run_adjoint_check  adjoint gradients vs FP64 central differences
+  run_precision Plummer-pair precision stress of the modes (errors, energy drift)
+  run_sweep     one step per graph replay over N = 2^4 .. 2^17
+  run_generate  scenario generation on the device; plugin start-up from a scenario
+  run_frontend  the reference's benchmark/worker protocol over its galaxy scenario
 """
 
 import statistics
@@ -395,3 +401,63 @@ def run_generate(n_big=1 << 24, n_plugin=1 << 17, reps=5, hbm_gbs=None, device=N
     out['plugin_start'] = {'n': n_plugin, 'scenario_s': t_scen, 'add_object_s': t_add,
                            'add_object_loop_s': t_objects, 'speedup': t_add / t_scen}
     return out
+
+
+def run_frontend(b_min=10, b_max=17, min_iterations=10, min_total_runtime=1.0, seed=0,
+                 device=None):
+    """The reference's benchmark over its galaxy scenario, measured the way its worker
+    measures a kernel, with the gb1 plugin as the kernel.
+
+    `gravitation benchmark -k gb1 -b 10 17` starts one worker per size 2^b
+    (cli/benchmark.py) on the galaxy scenario with stars_len = 2^b (simulation.py:57-77);
+    the worker (cli/worker.py:109-245) disables the garbage collector, and for each step
+    runs gc.collect(), times s.step() by wall clock (lib/timing.py:41-78, best_run_timer),
+    takes at least min_iterations steps, then more until min_total_runtime has passed,
+    and reports the best step time.  Here the universes start from the galaxy generated
+    on the device (the reference's generator is unseeded Python) with the recipe's
+    universe parameters; dtype float32 as in the scenario, so the plugin picks all pairs
+    below 8192 bodies and unique pairs above."""
+    import gc
+    from . import generate as gen
+    from .kernel import gb1
+    rows = []
+    for b in range(b_min, b_max + 1):
+        n = 1 << b
+        u = gb1.universe(scenario={'kind': 'galaxy', 'n': n, 'seed': seed}, dtype='float32',
+                         device=device, **gen.galaxy_universe_params())
+        u.start()
+        times = []
+        gc_was = gc.isenabled()
+        gc.disable()
+        try:
+            t_start = time.perf_counter_ns()
+
+            def one():
+                gc.collect()
+                t0 = time.perf_counter_ns()
+                u.step()
+                times.append(time.perf_counter_ns() - t0)
+                gc.collect()
+
+            for _ in range(min_iterations):
+                one()
+            elapsed = time.perf_counter_ns() - t_start
+            target = int(min_total_runtime * 1e9)
+            if elapsed < target:
+                for _ in range((target - elapsed) // elapsed * min_iterations):
+                    one()
+        finally:
+            if gc_was:
+                gc.enable()
+        mode = u._gb.mode_name
+        u.stop()
+        best = min(times)
+        rows.append({'n': n, 'mode': mode, 'steps': len(times), 'best_ns': best,
+                     'avg_ns': sum(times) // len(times),
+                     'interactions_per_s_best': n * n / (best * 1e-9)})
+    return {'workload': 'galaxy scenario (reference parameters), N = 2^%d..2^%d, worker '
+                        'protocol: gc off, gc.collect() between steps, wall clock, best of '
+                        '>= %d steps and >= %g s' % (b_min, b_max, min_iterations,
+                                                     min_total_runtime),
+            'path': 'gb1.universe.step(), host_sync=full (pm._r/pm._v valid after every step)',
+            'sizes': rows}

@@ -120,6 +120,20 @@ def test_precision_option_and_scaling(gpu, golden):
     assert np.median(oracle.rel_err_per_body(golden['gal_np1_f32_a0'], a)) < 1e-5
 
 
+def test_frontend_protocol_workload(gpu):
+    """The reference's worker protocol (gc off, gc.collect() between steps, best wall
+    time) over device-generated galaxies, small sizes."""
+    from gravitation_gb300.workloads import run_frontend
+    import gc
+    enabled = gc.isenabled()
+    out = run_frontend(b_min=6, b_max=9, min_iterations=3, min_total_runtime=0.01)
+    assert gc.isenabled() == enabled
+    assert [r['n'] for r in out['sizes']] == [64, 128, 256, 512]
+    for r in out['sizes']:
+        assert r['steps'] >= 3 and 0 < r['best_ns'] <= r['avg_ns']
+        assert r['mode'] == 'fp32'
+
+
 @pytest.mark.parametrize('sync', ['full', 'pull', 'none'])
 def test_graph_step_matches_launched_step(gpu, sync):
     """The graph-replayed fused step (default), the same work launched call by call,
