@@ -3,8 +3,9 @@
 
 Workload (default): one universe of N = 65536 bodies, positions U[-1000,1000]^3,
 velocities N(0,1), masses U[1,100] (seed 0), G = 6.6740831e-11, T = 1e3 -- FP32
-pairwise stage 1 with FP64 sums and FP64 stage 2 ("fp32" mode).  Synthetic data: the
-reference has no dataset, its own scenarios are generated too.
+pairwise stage 1 over unique pairs with compensated sums and FP64 stage 2 ("fp32u"
+mode; --mode picks another).  Synthetic data: the reference has no dataset, its own
+scenarios are generated too.
 
   value      pair interactions per second (N^2 per step), device-timed steps with the
              state resident in HBM; L2 flushed (256 MiB write) between timed steps

@@ -22,7 +22,7 @@
 // J slots), so stage 2 adds them like any partial sums (fixed order, deterministic).
 // Row sums are FP32 per tile, folded into compensated (TwoSum) FP32 hi+lo sums, as in
 // stage1_f32.cu, and go out as FP64; column sums are FP32 per tile and go out as FP32
-// (the first 3R floats of the slot), which stage 2 widens exactly.
+// (the first 3R floats of the slot), which stage 2 adds by TwoSum in FP32.
 #include "grav_device.cuh"
 
 namespace grav {
@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 				__syncthreads();
 				// column sums of this tile -> column slot of (I, J), then clear.  They are
 				// FP32 sums, so they go out as FP32 (first half of the slot; stage 2
-				// widens them exactly): half the bytes of an FP64 slot
+				// adds them by TwoSum in FP32): half the bytes of an FP64 slot
 				const int sJ = s + (blkJ - blkI);
 				const grav_seg_desc SJ = b.seg[sJ];
 				const int64_t slot = SJ.slot_base + SJ.nslots - (blkJ - blkI);

@@ -81,9 +81,14 @@ __global__ void __launch_bounds__(256) stage2_kernel(const grav_batch b, const i
 			ay += __ldg(p + IT);
 			az += __ldg(p + 2 * IT);
 		}
+		// column slots: FP32 values added in slot order by TwoSum in FP32 (hi + lo,
+		// ~48 bits) and widened once.  With FP64 adds and conversions per slot (64
+		// column slots per row at N = 65536) the FP64 pipe, ~1/64 of the FP32 rate on
+		// GB300, bound this kernel
 		const float* __restrict__ cpart =
 			reinterpret_cast<const float*>(b.part + static_cast<int64_t>(S.slot_base) * 3 * IT) + li;
 		const int64_t fstride = 2 * stride;  // floats per slot
+		float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
 		for (; k + SLOT_BATCH <= S.nslots; k += SLOT_BATCH) {
 			float px[SLOT_BATCH], py[SLOT_BATCH], pz[SLOT_BATCH];
 #pragma unroll
@@ -95,17 +100,20 @@ __global__ void __launch_bounds__(256) stage2_kernel(const grav_batch b, const i
 			}
 #pragma unroll
 			for (int q = 0; q < SLOT_BATCH; ++q) {
-				ax += static_cast<double>(px[q]);
-				ay += static_cast<double>(py[q]);
-				az += static_cast<double>(pz[q]);
+				two_sum_acc(hx, lx, px[q]);
+				two_sum_acc(hy, ly, py[q]);
+				two_sum_acc(hz, lz, pz[q]);
 			}
 		}
 		for (; k < S.nslots; ++k) {
 			const float* p = cpart + k * fstride;
-			ax += static_cast<double>(__ldg(p));
-			ay += static_cast<double>(__ldg(p + IT));
-			az += static_cast<double>(__ldg(p + 2 * IT));
+			two_sum_acc(hx, lx, __ldg(p));
+			two_sum_acc(hy, ly, __ldg(p + IT));
+			two_sum_acc(hz, lz, __ldg(p + 2 * IT));
 		}
+		ax += static_cast<double>(hx) + static_cast<double>(lx);
+		ay += static_cast<double>(hy) + static_cast<double>(ly);
+		az += static_cast<double>(hz) + static_cast<double>(lz);
 		if ((flags & GRAV_S2_WRITE_A) && b.a_out)
 			reinterpret_cast<drow4*>(b.a_out)[row] = drow4{ax, ay, az, 0.0};
 		if (flags & GRAV_S2_INTEGRATE) {

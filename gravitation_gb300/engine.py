@@ -6,9 +6,11 @@ one) and drives the persistent stage-1 kernel and the FP64 stage-2 kernel on a C
 stream.  There is no CPU path: without the library or a GB300 every call raises.
 
 Layout in HBM (all packed universe after universe):
-  r, v     float64 [n_bodies, 4]   (x, y, z, G*m) and (vx, vy, vz, 0)
-  pos      padded stage-1 positions: float4 hi (+ float4 lo in fp32c) or double4
-  part     float64 [n_slots, 3, itile]  FP64 partial sums written by stage 1
+  r, v     float64 [n_bodies, 4]   (x, y, z, G*m) and (vx, vy, vz, 0); or, after
+           bind_host_state, the caller's pinned host tensors of that layout
+  pos      padded stage-1 positions: float4 hi (+ float4 lo in fp32c/fp32cu) or double4
+  part     float64 [n_slots, 3, itile]  partial sums written by stage 1 (FP64 row
+           slots; the unique-pair column slots hold FP32 sums in their first half)
   univ/seg plan tables (grav_univ_desc / grav_seg_desc)
 """
 
@@ -134,7 +136,8 @@ class Engine:
     Parameters
       sizes : list of body counts (one per universe)
       T     : time step (scalar or one per universe)
-      mode  : 'fp32' (default), 'fp32c' or 'fp64'
+      mode  : 'fp32' (default, all pairs), 'fp32u' (unique pairs), 'fp32c' / 'fp32cu'
+              (compensated positions) or 'fp64'
       tile  : _lib.Tile, or None to use the autotuner's choice / the default shape
     """
 
@@ -144,7 +147,7 @@ class Engine:
         self.device = torch.device('cuda', self.dev_info.index)
         if isinstance(mode, str):
             if mode not in _lib.MODES:
-                raise ValueError('unknown precision mode %r (fp32, fp32c, fp64)' % mode)
+                raise ValueError('unknown precision mode %r (%s)' % (mode, ', '.join(_lib.MODES)))
             self.mode_name, self.mode = mode, _lib.MODES[mode]
         else:
             self.mode = int(mode)

@@ -117,8 +117,8 @@ class GB300Stages:
             n = len(self._mass_list)
         mode = meta.get('precision') or default_mode(self._dtype, n)
         if mode not in _lib.MODES:
-            raise ValueError('unsupported dtype/precision %r (float32, float64, fp32, fp32c, '
-                             'fp64)' % (meta.get('precision') or self._dtype,))
+            raise ValueError('unsupported dtype/precision %r (float32, float64, %s)' % (
+                meta.get('precision') or self._dtype, ', '.join(_lib.MODES)))
         self._gb_sync = meta.get('host_sync', 'full')
         if self._gb_sync not in ('full', 'pull', 'none'):
             raise ValueError('host_sync must be full, pull or none')

@@ -118,7 +118,7 @@ typedef struct grav_batch {
 	double* r;                    /* n_bodies x 4 */
 	double* v;                    /* n_bodies x 4 */
 	void* pos;                    /* padded stage-1 positions, grav_pos_bytes() */
-	double* part;                 /* n_slots x 3 x itile */
+	double* part;                 /* n_slots x 3 x itile (scratch of stage 1 -> stage 2) */
 	double* a_out;                /* n_bodies x 4, may be NULL unless GRAV_S2_WRITE_A */
 	int32_t* err;                 /* one device int, GRAV_DEV_* (first error wins) */
 } grav_batch;
