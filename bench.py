@@ -178,6 +178,13 @@ class ClockSampler:
                 'power_w_max': max(power), 'samples': len(sm), 'reasons': sorted(reasons)}
 
 
+def workload_name(n, mode):
+    """The headline workload, named the same by both arms."""
+    from gravitation_gb300.scenarios import G_DEFAULT, T_DEFAULT
+    return ('one universe, N=%d uniform cube seed 0, G=%.8g, T=%g, FP32 pair terms (%s on '
+            'the GPU) + FP64 stage 2' % (n, G_DEFAULT, T_DEFAULT, mode))
+
+
 # ---- CPU baseline (the reference's CPU design, restated portably) -------------------------
 
 def cpu_baseline_run(n, seed, target_s, runs=3):
@@ -226,8 +233,11 @@ def run_reference(args):
         'ms_per_step': 1e3 * args.n * args.n / value,
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
         'data': 'synthetic (seeded uniform cube)',
-        'config': {'workload': 'uniform cube N=%d seed 0, stage 1 FP32 (CPU)' % args.n,
-                   'n': args.n},
+        'config': {'workload': workload_name(args.n, args.mode), 'n': args.n,
+                   'mode': args.mode,
+                   'parallelism': 'CPU, %d OpenMP threads on the host cores' % threads,
+                   'timed': 'stage 1 (unique pairs, FP32); the O(N) stage 2 is under 1e-4 '
+                            'of a CPU step at this size and not timed'},
         'cpu_baseline': {'value': value, 'unit': UNIT, 'cores': threads, 'kind': 'port',
                          'sample': sample},
         'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
@@ -400,8 +410,7 @@ def run_ours(args):
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
         'dtype': 'f32 pair terms, f64 sums and stage 2',
         'data': 'synthetic (seeded uniform cube; the reference ships no dataset)',
-        'config': {'workload': 'one universe, N=%d uniform cube seed 0, G=%.8g, T=%g, %s '
-                               'stage 1 + FP64 stage 2' % (n, G_DEFAULT, T_DEFAULT, args.mode),
+        'config': {'workload': workload_name(n, args.mode),
                    'n': n, 'mode': args.mode,
                    'tile': {'bpt': eng.tile.bpt, 'threads': eng.tile.threads,
                             'jtile': eng.tile.jtile, 'grid': eng.info.grid},
