@@ -25,9 +25,10 @@ ADJ_TILE = (2, 128, 128)
 def default_adjoint_tile(sizes):
     """Tile of the backward pair kernel.  Up to ~10k bodies (1e8 ordered pairs) a step is
     latency bound and one body per thread (the finest work units) is fastest; above,
-    two bodies per thread.  Measured on GB300, backward step: N = 4096 -- 39.9 us with
-    (1, 128, 128), 41.6 us with (2, 128, 128); N = 65536 -- 5.16 ms with (2, 128, 128),
-    5.62 ms with (1, 128, 128)."""
+    two bodies per thread.  Measured on GB300, backward step: N = 4096 -- 37.8 us with
+    (1, 128, 128), 40.4 us with (2, 128, 128), 37.9 / 40.3 / 43.3 / 48.8 us with
+    (1, 64, 128) / (2, 64, 128) / (1, 128, 64) / (2, 64, 64); N = 65536 -- 5.16 ms with
+    (2, 128, 128), 5.62 ms with (1, 128, 128)."""
     if sum(int(n) * int(n) for n in sizes) <= 100_000_000:
         return (1, 128, 128)
     return ADJ_TILE

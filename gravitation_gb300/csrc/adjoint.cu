@@ -85,7 +85,7 @@ struct VjpOp {
 				const float inv = (r2 > 0.f) ? rsqrt_sfu(r2) : 0.f;
 				const float inv2 = inv * inv;
 				const float inv3 = inv2 * inv;
-				const float m3inv5 = inv3 * (-3.f * inv2);
+				const float inv5 = inv3 * inv2;  // the -3 of Jf is applied at the fold
 				const float c = pj.w * inv3;  // Gm_j / r^3
 				fa[0][k] = fmaf(c, dx, fa[0][k]);
 				fa[1][k] = fmaf(c, dy, fa[1][k]);
@@ -97,7 +97,7 @@ struct VjpOp {
 				const float duj = fmaf(dz, uj.z, fmaf(dy, uj.y, dx * uj.x));
 				const float duk = fmaf(dz, uzi[k], fmaf(dy, uyi[k], dx * uxi[k]));
 				const float dw = fmaf(gmi[k], duj, -pj.w * duk);
-				const float t = dw * m3inv5;
+				const float t = dw * inv5;
 				fq[0][k] = fmaf(t, dx, fq[0][k]);
 				fq[1][k] = fmaf(t, dy, fq[1][k]);
 				fq[2][k] = fmaf(t, dz, fq[2][k]);
@@ -115,8 +115,8 @@ struct VjpOp {
 			const float ui[3] = {uxi[k], uyi[k], uzi[k]};
 #pragma unroll
 			for (int c3 = 0; c3 < 3; ++c3) {
-				// h = Gm_k P - u_k S + Q   (the -3 is folded into t)
-				const float ht = fmaf(gmi[k], fp[c3][k], fmaf(-ui[c3], fs[k], fq[c3][k]));
+				// h = Gm_k P - u_k S - 3 Q
+				const float ht = fmaf(gmi[k], fp[c3][k], fmaf(-ui[c3], fs[k], -3.f * fq[c3][k]));
 				two_sum_acc(hh[c3][k], hl[c3][k], ht);
 				fp[c3][k] = fq[c3][k] = 0.f;
 			}
