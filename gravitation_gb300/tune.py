@@ -115,8 +115,12 @@ class Tuner:
             return self.tune(mode, sizes, dev_info)
         return default_tile(mode, sizes, dev_info.index)
 
-    def tune(self, mode, sizes, dev_info, reps=5, grid_factors=(1,)):
-        """Time every compiled tile shape on a seeded state and cache the fastest."""
+    def tune(self, mode, sizes, dev_info, reps=5, grid_factors=(1, 0.5, 0.25)):
+        """Time every compiled tile shape, with the persistent grid at each of
+        `grid_factors` x (SMs x resident CTAs), on a seeded state and cache the fastest.
+        What is timed is the full step (stage 1 + stage 2) replayed from a CUDA graph: a
+        smaller grid gives each CTA more work units but leaves fewer partial-sum slots
+        per row for stage 2, which at a few thousand bodies is worth as much."""
         import torch
         from .engine import Engine, occupancy, tile_list
         from .scenarios import uniform_cube
@@ -131,29 +135,34 @@ class Tuner:
         v = np.concatenate(vs) if vs else np.zeros((0, 3))
         gm = np.concatenate(ms) if ms else np.zeros(0)
         best = None
+        seen = set()
         for cand in tile_list(mode):
             occ = occupancy(mode, cand, dev_info.index)
             if occ <= 0:
                 continue
             for gf in grid_factors:
-                t = _lib.Tile(cand.bpt, cand.threads, cand.jtile, dev_info.sm_count * occ * gf)
+                grid = max(1, int(dev_info.sm_count * occ * gf))
+                t = _lib.Tile(cand.bpt, cand.threads, cand.jtile, grid)
                 eng = Engine(sizes, 1.0, mode=mode, tile=t, device=dev_info.index)
+                key = (t.bpt, t.threads, t.jtile, eng.info.grid)  # the plan caps the grid
+                if key in seen:
+                    continue
+                seen.add(key)
                 eng.set_state(r, v, gm)
                 s = torch.cuda.current_stream(eng.device)
-                eng.stage1()
-                eng.stage1()
+                g = eng.capture_graph(reps)
+                g.replay()
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(s)
-                for _ in range(reps):
-                    eng.stage1()
+                g.replay()
                 e1.record(s)
                 e1.synchronize()
                 eng.raise_on_device_error()
                 ms_ = e0.elapsed_time(e1) / reps
                 if best is None or ms_ < best[0]:
-                    best = (ms_, _lib.Tile(t.bpt, t.threads, t.jtile, t.grid))
-                del eng
+                    best = (ms_, _lib.Tile(t.bpt, t.threads, t.jtile, eng.info.grid))
+                del g, eng
         if best is None:
             raise RuntimeError('no tile shape could be timed for mode %s' % mode)
         self.store(mode, sizes, dev_info, best[1], best[0])

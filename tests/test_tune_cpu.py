@@ -1,0 +1,64 @@
+"""CPU tests of the tile autotuner's cache: size buckets, round trips, and robustness
+against corrupt files, stale builds and entries naming tiles that are not compiled."""
+
+import json
+import types
+
+import pytest
+
+from gravitation_gb300 import _lib, build as gbuild
+from gravitation_gb300.tune import Tuner, bucket_of
+
+DEV = types.SimpleNamespace(name='GB300 test', sm_count=152, index=0)
+
+
+@pytest.fixture(scope='module', autouse=True)
+def lib():
+    gbuild.build()
+    return _lib.load()
+
+
+def test_buckets():
+    assert bucket_of([1000]) == 'single:1024'
+    assert bucket_of([1024]) == 'single:1024'
+    assert bucket_of([1025]) == 'single:2048'
+    a, b = bucket_of([64, 128, 9000]), bucket_of([9000, 64, 128])
+    assert a == b and a.startswith('batch:3:')
+    assert bucket_of([64, 128, 9001]) != a
+
+
+def test_store_and_lookup(tmp_path):
+    t = Tuner(str(tmp_path / 'c.json'), build_hash='h1')
+    assert t.lookup('fp32', [4096], DEV) is None
+    t.store('fp32', [4096], DEV, _lib.Tile(1, 128, 128, 512), 0.02)
+    got = Tuner(str(tmp_path / 'c.json'), build_hash='h1').lookup('fp32', [4000], DEV)
+    assert (got.bpt, got.threads, got.jtile, got.grid) == (1, 128, 128, 512)
+    # another build of the library: the entry does not apply
+    assert Tuner(str(tmp_path / 'c.json'), build_hash='h2').lookup('fp32', [4096], DEV) is None
+    # another mode or size class
+    assert t.lookup('fp32u', [4096], DEV) is None
+    assert t.lookup('fp32', [8192], DEV) is None
+
+
+def test_corrupt_and_invalid_entries(tmp_path):
+    p = tmp_path / 'c.json'
+    p.write_text('{not json')
+    t = Tuner(str(p), build_hash='h')
+    assert t.lookup('fp32', [4096], DEV) is None
+    t.store('fp32', [4096], DEV, _lib.Tile(1, 128, 128, 64), 0.01)   # rewrites the file
+    assert json.loads(p.read_text())['format'] == 1
+    data = json.loads(p.read_text())
+    key = t.key('fp32', [4096], DEV)
+    for bad in ({'bpt': 3, 'threads': 128, 'jtile': 128, 'grid': 64},   # not compiled
+                {'bpt': 1, 'threads': 128, 'jtile': 128, 'grid': 0},    # no grid
+                {'bpt': 'x'}, 'garbage'):
+        data['entries'][key] = bad
+        p.write_text(json.dumps(data))
+        assert Tuner(str(p), build_hash='h').lookup('fp32', [4096], DEV) is None
+
+
+def test_choose_without_tuning_uses_the_cache(tmp_path):
+    t = Tuner(str(tmp_path / 'c.json'), build_hash='h')
+    t.store('fp32u', [65536], DEV, _lib.Tile(8, 128, 256, 456), 1.3)
+    got = t.choose('fp32u', [65536], DEV, tune_if_missing=False)
+    assert (got.bpt, got.threads, got.jtile, got.grid) == (8, 128, 256, 456)
