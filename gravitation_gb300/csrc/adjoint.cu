@@ -25,7 +25,7 @@
 // Pair kernel: persistent stage-1 work list (pairs_skeleton.cuh), j-tiles of FP32
 // positions (x, y, z, Gm) and FP32 u, FP32 tile partials folded into compensated
 // (TwoSum) FP32 sums, so no FP64 arithmetic runs in the pair loop; 7 outputs
-// per body (a, h, g) in the partial slots.  Adjoint stage 2 (one thread per padded row)
+// per body (a, h, g) in the partial slots.  Adjoint stage 2 (1 or 8 lanes per padded row)
 // sums the slots and applies the updates above in FP64, then prepares the FP32
 // positions r_{k-1} and u for the next backward step.
 #include "pairs_skeleton.cuh"
@@ -159,11 +159,24 @@ struct __align__(32) arow4 {
 #define ADJ_STEP 1     // apply one backward step from the pair kernel's sums
 #define ADJ_PREPARE 2  // write FP32 r_{k-1} = r - T v and u = gv + T gr for the pair kernel
 
-__global__ void __launch_bounds__(256) adjoint_stage2_kernel(const grav_batch b, double* gr,
-	double* gv, double* ggm, float4* upos, const int flags)
+// Lanes per row, as in stage2.cu: for small batches the row's slots are split over
+// ATPR adjacent lanes of a warp (lane p takes slots p, p + ATPR, ...) and combined by a
+// butterfly, which gives every lane the same bits; lane 0 then applies the row's
+// update.  Large batches use one lane per row (the combining adds are FP64).
+constexpr int AS2_THREADS = 128;
+constexpr int ADJ_SPLIT_ROWS_MAX = 16384;  // ATPR = 8 up to this many padded rows, else 1
+
+template <int ATPR>
+__global__ void __launch_bounds__(AS2_THREADS) adjoint_stage2_kernel(const grav_batch b,
+	double* gr, double* gv, double* ggm, float4* upos, const int flags)
 {
-	const int64_t g = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-	if (g >= b.n_pad_total) return;
+	static_assert(ATPR > 0 && ATPR <= 16 && (ATPR & (ATPR - 1)) == 0 && AS2_THREADS % 32 == 0,
+		"a row's lanes must sit in one warp");
+	const int64_t gthread = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+	const int64_t g = gthread / ATPR;  // padded row; the ATPR lanes of a row share a warp
+	const int p = static_cast<int>(gthread % ATPR);
+	const unsigned gmask = ((1u << ATPR) - 1) << ((threadIdx.x & 31) & ~(ATPR - 1));
+	if (g >= b.n_pad_total) return;  // the whole lane group
 	const int IT = b.tile.bpt * b.tile.threads;
 	const int64_t seg = g / IT;
 	const int li = static_cast<int>(g - seg * IT);
@@ -173,9 +186,11 @@ __global__ void __launch_bounds__(256) adjoint_stage2_kernel(const grav_batch b,
 	// slots, state, gradients and positions belong to the kernels before this one
 	grid_dep_wait();
 	float4* pos = static_cast<float4*>(b.pos);
-	if (il >= U.n) {
-		pos[g] = make_float4(0.f, 0.f, 0.f, 0.f);
-		upos[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+	if (il >= U.n) {  // the whole lane group
+		if (p == 0) {
+			pos[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+			upos[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+		}
 		return;
 	}
 	const int64_t row = U.body_off + il;
@@ -184,29 +199,46 @@ __global__ void __launch_bounds__(256) adjoint_stage2_kernel(const grav_batch b,
 	arow4* vv = reinterpret_cast<arow4*>(b.v);
 	arow4* grr = reinterpret_cast<arow4*>(gr);
 	arow4* gvv = reinterpret_cast<arow4*>(gv);
-	arow4 r = rr[row], v = vv[row], a_gr = grr[row], a_gv = gvv[row];
+	// lane 0 owns the row's update: its loads go out before the slot loads
+	arow4 r = {0.0, 0.0, 0.0, 0.0}, v = r, a_gr = r, a_gv = r;
+	if (p == 0) {
+		r = rr[row];
+		v = vv[row];
+		a_gr = grr[row];
+		a_gv = gvv[row];
+	}
 
+	double s[7] = {0, 0, 0, 0, 0, 0, 0};
 	if (flags & ADJ_STEP) {
-		// slots added in slot order, their loads issued SLOT_BATCH slots at a time
+		// slots p, p + ATPR, ... added in order; each round issues all its loads first
+		// (the ones past the end are skipped), so a short list costs one latency
 		constexpr int SLOT_BATCH = 4;
-		double s[7] = {0, 0, 0, 0, 0, 0, 0};
 		const double* part = b.part + static_cast<int64_t>(S.slot_base) * 7 * IT + li;
-		int k = 0;
-		for (; k + SLOT_BATCH <= S.nslots; k += SLOT_BATCH) {
+		for (int k = p; k < S.nslots; k += SLOT_BATCH * ATPR) {
+			const int m = min(SLOT_BATCH, (S.nslots - k + ATPR - 1) / ATPR);
 			double q[SLOT_BATCH][7];
 #pragma unroll
 			for (int j = 0; j < SLOT_BATCH; ++j)
+				if (j < m) {
 #pragma unroll
-				for (int c = 0; c < 7; ++c) q[j][c] = __ldg(part + (static_cast<int64_t>(k + j) * 7 + c) * IT);
+					for (int c = 0; c < 7; ++c)
+						q[j][c] = __ldg(part + (static_cast<int64_t>(k + j * ATPR) * 7 + c) * IT);
+				}
 #pragma unroll
 			for (int j = 0; j < SLOT_BATCH; ++j)
+				if (j < m) {
 #pragma unroll
-				for (int c = 0; c < 7; ++c) s[c] += q[j][c];
+					for (int c = 0; c < 7; ++c) s[c] += q[j][c];
+				}
 		}
-		for (; k < S.nslots; ++k) {
 #pragma unroll
-			for (int c = 0; c < 7; ++c) s[c] += __ldg(part + (static_cast<int64_t>(k) * 7 + c) * IT);
-		}
+		for (int o = 1; o < ATPR; o <<= 1)
+#pragma unroll
+			for (int c = 0; c < 7; ++c) s[c] += __shfl_xor_sync(gmask, s[c], o);
+	}
+	if (p != 0) return;
+
+	if (flags & ADJ_STEP) {
 		// reverse the forward update: r_k = r_{k+1} - T v_{k+1}; v_k = v_{k+1} - T a_k
 		r.x = __dsub_rn(r.x, __dmul_rn(v.x, T));
 		r.y = __dsub_rn(r.y, __dmul_rn(v.y, T));
@@ -241,7 +273,7 @@ __global__ void __launch_bounds__(256) adjoint_stage2_kernel(const grav_batch b,
 }
 
 // Adjoint stage 2 as a programmatic dependent of the kernel before it (it waits with
-// grid_dep_wait); small CTAs so that a few thousand rows still spread over many SMs.
+// grid_dep_wait); 8 lanes per padded row for small batches, else 1.
 cudaError_t launch_adjoint_stage2(const grav_batch& b, const grav_adjoint& a, int flags,
 	cudaStream_t st)
 {
@@ -252,9 +284,12 @@ cudaError_t launch_adjoint_stage2(const grav_batch& b, const grav_adjoint& a, in
 	float4* upos = static_cast<float4*>(a.upos);
 	int f = flags;
 	void* args[] = {&copy, &gr, &gv, &ggm, &upos, &f};
-	const unsigned blocks = static_cast<unsigned>((b.n_pad_total + 63) / 64);
-	return launch_dependent(reinterpret_cast<const void*>(&adjoint_stage2_kernel), blocks, 64, 0,
-		st, args);
+	const int atpr = b.n_pad_total <= ADJ_SPLIT_ROWS_MAX ? 8 : 1;
+	const unsigned blocks =
+		static_cast<unsigned>((b.n_pad_total * atpr + AS2_THREADS - 1) / AS2_THREADS);
+	const void* fn = atpr == 8 ? reinterpret_cast<const void*>(&adjoint_stage2_kernel<8>)
+	                           : reinterpret_cast<const void*>(&adjoint_stage2_kernel<1>);
+	return launch_dependent(fn, blocks, AS2_THREADS, 0, st, args);
 }
 
 struct VjpKernel {

@@ -1,8 +1,9 @@
 // stage2.cu -- stage 2 of the step and the refresh of the stage-1 positions.
 //
-// One thread per row of the padded position array.  For a real body it adds the
-// FP64 partial-sum slots of its segment in slot order (deterministic), then applies
-// the base class's update in FP64 with separately rounded products and sums,
+// One or TPR lanes per row of the padded position array.  For a real body they add the
+// partial-sum slots of its segment (each lane its share, in slot order, then a fixed
+// butterfly: deterministic), then lane 0 applies the base class's update in FP64 with
+// separately rounded products and sums,
 //     v = a*T + v ;  r = v*T + r          (_base_.py:58-62, np2.py:110-115)
 // exactly as the reference's Python floats / numpy arrays round them, and finally
 // rewrites the row of the stage-1 position array (FP32 hi[, lo] or FP64).  Padding
@@ -15,13 +16,30 @@ struct __align__(32) drow4 {
 	double x, y, z, w;
 };
 
-__global__ void __launch_bounds__(256) stage2_kernel(const grav_batch b, const int flags)
+// Lanes per row: for small batches the row's slots are split over TPR adjacent lanes
+// of a warp (lane p takes slots p, p + TPR, ...), so a few dozen slots cost one round
+// of memory latency, and the lanes' partial sums are combined by a butterfly, which
+// gives every lane the same bits (each addition pairs the same two operands on both
+// sides).  For large batches one lane per row: the extra lanes' FP64 combining adds
+// and conversions would run on GB300's FP64 pipe (~1/64 of the FP32 rate).
+constexpr int S2_THREADS = 128;
+constexpr int SPLIT_ROWS_MAX = 32768;  // TPR = 4 up to this many padded rows, else 1
+constexpr int ROW_BATCH = 8;           // FP64 row-slot loads in flight per lane
+constexpr int COL_BATCH = 16;          // FP32 column-slot loads in flight per lane
+
+template <int TPR>
+__global__ void __launch_bounds__(S2_THREADS) stage2_kernel(const grav_batch b, const int flags)
 {
+	static_assert(TPR > 0 && TPR <= 16 && (TPR & (TPR - 1)) == 0 && S2_THREADS % 32 == 0,
+		"a row's lanes must sit in one warp");
 	// launched as a dependent of stage 1; the next stage 1 may start launching when
 	// this grid's CTAs exit (no earlier trigger: the persistent stage-1 grid should
 	// find its SMs free)
-	const int64_t g = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-	if (g >= b.n_pad_total) return;
+	const int64_t gthread = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+	const int64_t g = gthread / TPR;  // padded row; the TPR lanes of a row share a warp
+	const int p = static_cast<int>(gthread % TPR);
+	const unsigned gmask = ((1u << TPR) - 1) << ((threadIdx.x & 31) & ~(TPR - 1));
+	if (g >= b.n_pad_total) return;  // the whole lane group
 	const int IT = b.tile.bpt * b.tile.threads;
 	const int64_t seg = g / IT;
 	const int li = static_cast<int>(g - seg * IT);
@@ -31,94 +49,106 @@ __global__ void __launch_bounds__(256) stage2_kernel(const grav_batch b, const i
 	// slots, positions and the state belong to the kernels before this one
 	grid_dep_wait();
 
-	if (il >= U.n) {
+	if (il >= U.n) {  // the whole lane group
+		if (p != 0) return;
 		if (b.mode == GRAV_MODE_FP64) {
 			static_cast<drow4*>(b.pos)[g] = drow4{0.0, 0.0, 0.0, 0.0};
 		} else {
-			float4* p = static_cast<float4*>(b.pos);
-			p[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+			float4* q = static_cast<float4*>(b.pos);
+			q[g] = make_float4(0.f, 0.f, 0.f, 0.f);
 			if (b.mode == GRAV_MODE_FP32C || b.mode == GRAV_MODE_FP32CU)
-				p[b.n_pad_total + g] = make_float4(0.f, 0.f, 0.f, 0.f);
+				q[b.n_pad_total + g] = make_float4(0.f, 0.f, 0.f, 0.f);
 		}
 		return;
 	}
 
 	const int64_t row = U.body_off + il;
 	drow4* rr = reinterpret_cast<drow4*>(b.r);
-	drow4 r = rr[row];
+	drow4* vv = reinterpret_cast<drow4*>(b.v);
+	const bool integrate = !(flags & GRAV_S2_PREPARE) && (flags & GRAV_S2_INTEGRATE);
+	// lane 0 owns the row's update: its state loads go out before the slot loads
+	drow4 r = {0.0, 0.0, 0.0, 0.0}, v = {0.0, 0.0, 0.0, 0.0};
+	if (p == 0) {
+		r = rr[row];
+		if (integrate) v = vv[row];
+	}
 
+	double ax = 0.0, ay = 0.0, az = 0.0;
 	if (!(flags & GRAV_S2_PREPARE)) {
-		// slots are added in slot order; their loads are issued SLOT_BATCH at a time so
-		// that a long slot list costs a few memory latencies, not one per slot
-		constexpr int SLOT_BATCH = 8;
-		double ax = 0.0, ay = 0.0, az = 0.0;
-		const double* __restrict__ part = b.part + static_cast<int64_t>(S.slot_base) * 3 * IT + li;
 		const int64_t stride = 3 * static_cast<int64_t>(IT);
+		const double* __restrict__ part = b.part + static_cast<int64_t>(S.slot_base) * stride + li;
 		// unique-pair plans: the last (row block index) slots of a segment are column
 		// slots holding FP32 sums in their first half (stage1_sym.cu)
 		const bool pairs = b.mode == GRAV_MODE_FP32U || b.mode == GRAV_MODE_FP32CU;
 		const int nrow = pairs ? S.nslots - S.il0 / IT : S.nslots;
-		int k = 0;
-		for (; k + SLOT_BATCH <= nrow; k += SLOT_BATCH) {
-			double px[SLOT_BATCH], py[SLOT_BATCH], pz[SLOT_BATCH];
+		// FP64 row slots p, p + TPR, ... added in order; each round issues all its loads
+		// first (the ones past the end are skipped), so a short list costs one latency
+		for (int k = p; k < nrow; k += ROW_BATCH * TPR) {
+			const int m = min(ROW_BATCH, (nrow - k + TPR - 1) / TPR);
+			double px[ROW_BATCH], py[ROW_BATCH], pz[ROW_BATCH];
 #pragma unroll
-			for (int q = 0; q < SLOT_BATCH; ++q) {
-				const double* p = part + (k + q) * stride;
-				px[q] = __ldg(p);
-				py[q] = __ldg(p + IT);
-				pz[q] = __ldg(p + 2 * IT);
+			for (int q = 0; q < ROW_BATCH; ++q) {
+				if (q < m) {
+					const double* ps = part + (k + q * TPR) * stride;
+					px[q] = __ldg(ps);
+					py[q] = __ldg(ps + IT);
+					pz[q] = __ldg(ps + 2 * IT);
+				}
 			}
 #pragma unroll
-			for (int q = 0; q < SLOT_BATCH; ++q) {
-				ax += px[q];
-				ay += py[q];
-				az += pz[q];
+			for (int q = 0; q < ROW_BATCH; ++q) {
+				if (q < m) {
+					ax += px[q];
+					ay += py[q];
+					az += pz[q];
+				}
 			}
 		}
-		for (; k < nrow; ++k) {
-			const double* p = part + k * stride;
-			ax += __ldg(p);
-			ay += __ldg(p + IT);
-			az += __ldg(p + 2 * IT);
-		}
-		// column slots: FP32 values added in slot order by TwoSum in FP32 (hi + lo,
-		// ~48 bits) and widened once.  With FP64 adds and conversions per slot (64
-		// column slots per row at N = 65536) the FP64 pipe, ~1/64 of the FP32 rate on
-		// GB300, bound this kernel
-		const float* __restrict__ cpart =
-			reinterpret_cast<const float*>(b.part + static_cast<int64_t>(S.slot_base) * 3 * IT) + li;
-		const int64_t fstride = 2 * stride;  // floats per slot
-		float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
-		for (; k + SLOT_BATCH <= S.nslots; k += SLOT_BATCH) {
-			float px[SLOT_BATCH], py[SLOT_BATCH], pz[SLOT_BATCH];
+		if (pairs) {
+			// FP32 column slots: added by TwoSum in FP32 (hi + lo, ~48 bits) and widened
+			// once; FP64 adds per slot would run on GB300's FP64 pipe.  Loads past the end
+			// read as 0, which TwoSum adds exactly
+			const float* __restrict__ cpart =
+				reinterpret_cast<const float*>(b.part + static_cast<int64_t>(S.slot_base) * stride) + li;
+			const int64_t fstride = 2 * stride;  // floats per slot
+			float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
+			for (int k = nrow + p; k < S.nslots; k += COL_BATCH * TPR) {
+				float px[COL_BATCH], py[COL_BATCH], pz[COL_BATCH];
 #pragma unroll
-			for (int q = 0; q < SLOT_BATCH; ++q) {
-				const float* p = cpart + (k + q) * fstride;
-				px[q] = __ldg(p);
-				py[q] = __ldg(p + IT);
-				pz[q] = __ldg(p + 2 * IT);
-			}
+				for (int q = 0; q < COL_BATCH; ++q) {
+					px[q] = py[q] = pz[q] = 0.f;
+					if (k + q * TPR < S.nslots) {
+						const float* ps = cpart + (k + q * TPR) * fstride;
+						px[q] = __ldg(ps);
+						py[q] = __ldg(ps + IT);
+						pz[q] = __ldg(ps + 2 * IT);
+					}
+				}
 #pragma unroll
-			for (int q = 0; q < SLOT_BATCH; ++q) {
-				two_sum_acc(hx, lx, px[q]);
-				two_sum_acc(hy, ly, py[q]);
-				two_sum_acc(hz, lz, pz[q]);
+				for (int q = 0; q < COL_BATCH; ++q) {
+					two_sum_acc(hx, lx, px[q]);
+					two_sum_acc(hy, ly, py[q]);
+					two_sum_acc(hz, lz, pz[q]);
+				}
 			}
+			ax += static_cast<double>(hx) + static_cast<double>(lx);
+			ay += static_cast<double>(hy) + static_cast<double>(ly);
+			az += static_cast<double>(hz) + static_cast<double>(lz);
 		}
-		for (; k < S.nslots; ++k) {
-			const float* p = cpart + k * fstride;
-			two_sum_acc(hx, lx, __ldg(p));
-			two_sum_acc(hy, ly, __ldg(p + IT));
-			two_sum_acc(hz, lz, __ldg(p + 2 * IT));
+		// combine the lanes' sums: ((s0 + s1) + (s2 + s3)) on every lane
+#pragma unroll
+		for (int o = 1; o < TPR; o <<= 1) {
+			ax += __shfl_xor_sync(gmask, ax, o);
+			ay += __shfl_xor_sync(gmask, ay, o);
+			az += __shfl_xor_sync(gmask, az, o);
 		}
-		ax += static_cast<double>(hx) + static_cast<double>(lx);
-		ay += static_cast<double>(hy) + static_cast<double>(ly);
-		az += static_cast<double>(hz) + static_cast<double>(lz);
+	}
+	if (p != 0) return;
+
+	if (!(flags & GRAV_S2_PREPARE)) {
 		if ((flags & GRAV_S2_WRITE_A) && b.a_out)
 			reinterpret_cast<drow4*>(b.a_out)[row] = drow4{ax, ay, az, 0.0};
-		if (flags & GRAV_S2_INTEGRATE) {
-			drow4* vv = reinterpret_cast<drow4*>(b.v);
-			drow4 v = vv[row];
+		if (integrate) {
 			const double T = U.T;
 			v.x = __dadd_rn(__dmul_rn(ax, T), v.x);
 			v.y = __dadd_rn(__dmul_rn(ay, T), v.y);
@@ -134,13 +164,13 @@ __global__ void __launch_bounds__(256) stage2_kernel(const grav_batch b, const i
 	if (b.mode == GRAV_MODE_FP64) {
 		static_cast<drow4*>(b.pos)[g] = r;
 	} else {
-		float4* p = static_cast<float4*>(b.pos);
+		float4* q = static_cast<float4*>(b.pos);
 		const float hx = __double2float_rn(r.x);
 		const float hy = __double2float_rn(r.y);
 		const float hz = __double2float_rn(r.z);
-		p[g] = make_float4(hx, hy, hz, __double2float_rn(r.w));
+		q[g] = make_float4(hx, hy, hz, __double2float_rn(r.w));
 		if (b.mode == GRAV_MODE_FP32C || b.mode == GRAV_MODE_FP32CU) {
-			p[b.n_pad_total + g] = make_float4(
+			q[b.n_pad_total + g] = make_float4(
 				__double2float_rn(__dsub_rn(r.x, static_cast<double>(hx))),
 				__double2float_rn(__dsub_rn(r.y, static_cast<double>(hy))),
 				__double2float_rn(__dsub_rn(r.z, static_cast<double>(hz))), 0.f);
@@ -151,14 +181,14 @@ __global__ void __launch_bounds__(256) stage2_kernel(const grav_batch b, const i
 cudaError_t launch_stage2(const grav_batch& b, int flags, cudaStream_t stream)
 {
 	if (b.n_pad_total == 0) return cudaSuccess;
-	// small CTAs: a few thousand rows still spread over many SMs (latency bound)
-	const int threads = 64;
-	const int64_t blocks = (b.n_pad_total + threads - 1) / threads;
+	const int tpr = b.n_pad_total <= SPLIT_ROWS_MAX ? 4 : 1;
+	const int64_t blocks = (b.n_pad_total * tpr + S2_THREADS - 1) / S2_THREADS;
 	grav_batch copy = b;
 	int f = flags;
 	void* args[] = {&copy, &f};
-	return launch_dependent(reinterpret_cast<const void*>(&stage2_kernel),
-		static_cast<unsigned>(blocks), threads, 0, stream, args);
+	const void* fn = tpr == 4 ? reinterpret_cast<const void*>(&stage2_kernel<4>)
+	                          : reinterpret_cast<const void*>(&stage2_kernel<1>);
+	return launch_dependent(fn, static_cast<unsigned>(blocks), S2_THREADS, 0, stream, args);
 }
 
 }  // namespace grav
