@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, 'libgravgb300.so')
 
 # ---- constants (mirror of the header) -------------------------------------------
-GRAV_ABI_VERSION = 1
+GRAV_ABI_VERSION = 2
 GRAV_OK = 0
 GRAV_E_ARG = -1
 GRAV_E_TILE = -2
@@ -130,8 +130,8 @@ _DECLS = {
     'grav_scenario_scratch_bytes': (ctypes.c_int64, [_P(Scenario), ctypes.c_int64]),
     'grav_scenario_generate': (ctypes.c_int, [_P(Scenario), ctypes.c_void_p, ctypes.c_void_p,
                                               ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]),
-    'grav_adjoint_tile_supported': (ctypes.c_int, [_P(Tile)]),
-    'grav_adjoint_occupancy': (ctypes.c_int, [_P(Tile), _P(ctypes.c_int32)]),
+    'grav_adjoint_tile_supported': (ctypes.c_int, [ctypes.c_int, _P(Tile)]),
+    'grav_adjoint_occupancy': (ctypes.c_int, [ctypes.c_int, _P(Tile), _P(ctypes.c_int32)]),
     'grav_adjoint_prepare': (ctypes.c_int, [_P(Adjoint), ctypes.c_void_p]),
     'grav_adjoint_step': (ctypes.c_int, [_P(Adjoint), ctypes.c_void_p]),
     'grav_forces_noalloc': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,

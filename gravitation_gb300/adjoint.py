@@ -22,36 +22,56 @@ from .engine import Engine, device_info, make_plan, _ctypes_to_device
 ADJ_TILE = (2, 128, 128)
 
 
-def default_adjoint_tile(sizes):
-    """Tile of the backward pair kernel.  Up to ~10k bodies (1e8 ordered pairs) a step is
+def default_adjoint_pairs(sizes):
+    """The unique-pair backward kernel from ~6k bodies (4e7 ordered pairs) on.  Measured
+    on GB300, backward step (graph-replayed) all pairs vs unique pairs: N = 4096 --
+    32.8 vs 32.4 us (no gain: the unique-pair units are too coarse there), N = 8192 --
+    117 vs 95 us, N = 16384 -- 385 vs 313 us, N = 65536 -- 5.63 vs 4.15 ms."""
+    return sum(int(n) * int(n) for n in sizes) >= 40_000_000
+
+
+def default_adjoint_tile(sizes, pairs=False):
+    """Tile of the backward pair kernel.  All pairs: up to ~10k bodies (1e8 ordered pairs) a step is
     latency bound and one body per thread (the finest work units) is fastest; above,
     two bodies per thread.  Measured on GB300, backward step: N = 4096 -- 37.8 us with
     (1, 128, 128), 40.4 us with (2, 128, 128), 37.9 / 40.3 / 43.3 / 48.8 us with
     (1, 64, 128) / (2, 64, 128) / (1, 128, 64) / (2, 64, 64); N = 65536 -- 5.16 ms with
     (2, 128, 128), 5.62 ms with (1, 128, 128)."""
+    if pairs:
+        # unique pairs: 2 rows/thread and 64-body j-tiles up to ~20k bodies, 4 and 128 above
+        return (2, 128, 64) if sum(int(n) * int(n) for n in sizes) <= 400_000_000 else (4, 128, 128)
     if sum(int(n) * int(n) for n in sizes) <= 100_000_000:
         return (1, 128, 128)
     return ADJ_TILE
 
 
 class AdjointEngine:
-    """Buffers and plan of the backward sweep for a packed batch of universes."""
+    """Buffers and plan of the backward sweep for a packed batch of universes.
 
-    def __init__(self, sizes, T, device=None, tile=None):
+    pairs: True -- the unique-pair backward kernel (each unordered pair once, plan of
+    grav_plan_pairs); False -- every ordered pair (plan of grav_plan); None -- by size.
+    tile: (bpt, threads, jtile) of that kernel, default by size."""
+
+    def __init__(self, sizes, T, device=None, tile=None, pairs=None):
         self.lib = _lib.load()
         self.dev_info = device_info(device)
         self.device = torch.device('cuda', self.dev_info.index)
         self.sizes = [int(n) for n in sizes]
+        if pairs is None:
+            pairs = default_adjoint_pairs(self.sizes)
+        self.pairs = bool(pairs)
+        mode = _lib.GRAV_MODE_FP32U if self.pairs else _lib.GRAV_MODE_FP32
         if tile is None:
-            tile = default_adjoint_tile(self.sizes)
+            tile = default_adjoint_tile(self.sizes, self.pairs)
         t = _lib.Tile(tile[0], tile[1], tile[2], 0)
-        if not self.lib.grav_adjoint_tile_supported(ctypes.byref(t)):
-            raise ValueError('no adjoint kernel for tile %r' % (tile,))
+        if not self.lib.grav_adjoint_tile_supported(mode, ctypes.byref(t)):
+            raise ValueError('no %s adjoint kernel for tile %r' % (
+                'unique-pair' if self.pairs else 'all-pairs', tile))
         occ = ctypes.c_int32()
         with torch.cuda.device(self.device):
-            check(self.lib.grav_adjoint_occupancy(ctypes.byref(t), ctypes.byref(occ)))
+            check(self.lib.grav_adjoint_occupancy(mode, ctypes.byref(t), ctypes.byref(occ)))
         t.grid = self.dev_info.sm_count * max(occ.value, 1)
-        self.info, univ, seg = make_plan(self.sizes, T, t)
+        self.info, univ, seg = make_plan(self.sizes, T, t, 'fp32u' if self.pairs else 'fp32')
         info, dev = self.info, self.device
         self.univ_dev = _ctypes_to_device(univ, ctypes.sizeof(_lib.UnivDesc) * info.n_univ, dev)
         self.seg_dev = _ctypes_to_device(seg, ctypes.sizeof(_lib.SegDesc) * info.n_seg, dev)
@@ -67,7 +87,7 @@ class AdjointEngine:
         self.part7 = torch.zeros(max(info.n_slots * 7 * info.itile, 1), **f64)
         self.err = torch.zeros(1, dtype=torch.int32, device=dev)
         b = _lib.Batch()
-        b.mode = _lib.GRAV_MODE_FP32
+        b.mode = mode
         b.n_univ, b.n_seg, b.n_slots = info.n_univ, info.n_seg, info.n_slots
         b.n_bodies, b.n_pad_total, b.n_units = info.n_bodies, info.n_pad_total, info.n_units
         b.tile = _lib.Tile(t.bpt, t.threads, t.jtile, info.grid)
@@ -109,14 +129,19 @@ class Rollout:
     """Forward engine + adjoint engine for one batch of universes (reusable)."""
 
     def __init__(self, sizes, T, steps, every=32, device=None, fwd_tile=None, tuner=None,
-                 mode='fp32', graphs=True):
+                 mode=None, graphs=True, adj_pairs=None):
         self.sizes = [int(n) for n in sizes]
         self.T = float(T)
         self.steps = int(steps)
         self.every = max(1, int(every))
+        if mode is None:
+            # the forward's FP32 kernel by size, as the plugin picks it: all pairs for
+            # small universes, unique pairs from 8192 bodies
+            from .plugin import default_mode
+            mode = default_mode('float32', max(self.sizes))
         self.fwd = Engine(self.sizes, self.T, mode=mode, tile=fwd_tile, device=device,
                           tuner=tuner)
-        self.adj = AdjointEngine(self.sizes, self.T, device=device)
+        self.adj = AdjointEngine(self.sizes, self.T, device=device, pairs=adj_pairs)
         self.graphs = bool(graphs)
         self._fwd_graphs = {}
         self._adj_graphs = {}

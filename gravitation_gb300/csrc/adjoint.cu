@@ -25,7 +25,7 @@
 // Pair kernel: persistent stage-1 work list (pairs_skeleton.cuh), j-tiles of FP32
 // positions (x, y, z, Gm) and FP32 u, FP32 tile partials folded into compensated
 // (TwoSum) FP32 sums, so no FP64 arithmetic runs in the pair loop; 7 outputs
-// per body (a, h, g) in the partial slots.  Adjoint stage 2 (1 or 8 lanes per padded row)
+// per body (a, h, g) in the partial slots, as FP32 (hi, lo) pairs.  Adjoint stage 2 (1 or 8 lanes per padded row)
 // sums the slots and applies the updates above in FP64, then prepares the FP32
 // positions r_{k-1} and u for the next backward step.
 #include "pairs_skeleton.cuh"
@@ -33,6 +33,9 @@
 namespace grav {
 
 int record_error(int code, const char* msg);
+// the unique-pair backward pair kernel (adjoint_sym.cu)
+cudaError_t launch_vjp_sym(const grav_batch& b, const float4* upos, cudaStream_t st);
+int vjp_sym_occupancy(int bpt, int threads, int jtile, int* ctas_per_sm);
 
 template <int B_, int T_, int J_>
 struct VjpOp {
@@ -125,19 +128,21 @@ struct VjpOp {
 		}
 	}
 
+	// the compensated sums go out as FP32 (hi, lo) pairs, one 8-byte slot entry each, with
+	// no FP64 arithmetic; the adjoint stage 2 adds them in FP32 by TwoSum
 	__device__ void store(double* out, int tid)
 	{
 		constexpr int IT = B * T;
+		float2* out2 = reinterpret_cast<float2*>(out);
 #pragma unroll
 		for (int k = 0; k < B; ++k) {
 			const int i = tid + k * T;
 #pragma unroll
 			for (int c3 = 0; c3 < 3; ++c3) {
-				out[c3 * IT + i] = static_cast<double>(ah[c3][k]) + static_cast<double>(al[c3][k]);
-				out[(3 + c3) * IT + i] =
-					static_cast<double>(hh[c3][k]) + static_cast<double>(hl[c3][k]);
+				out2[c3 * IT + i] = make_float2(ah[c3][k], al[c3][k]);
+				out2[(3 + c3) * IT + i] = make_float2(hh[c3][k], hl[c3][k]);
 			}
-			out[6 * IT + i] = static_cast<double>(gh[k]) + static_cast<double>(gl[k]);
+			out2[6 * IT + i] = make_float2(gh[k], gl[k]);
 		}
 	}
 };
@@ -162,7 +167,7 @@ struct __align__(32) arow4 {
 // Lanes per row, as in stage2.cu: for small batches the row's slots are split over
 // ATPR adjacent lanes of a warp (lane p takes slots p, p + ATPR, ...) and combined by a
 // butterfly, which gives every lane the same bits; lane 0 then applies the row's
-// update.  Large batches use one lane per row (the combining adds are FP64).
+// update.  Large batches use one lane per row.
 constexpr int AS2_THREADS = 128;
 constexpr int ADJ_SPLIT_ROWS_MAX = 16384;  // ATPR = 8 up to this many padded rows, else 1
 
@@ -210,31 +215,58 @@ __global__ void __launch_bounds__(AS2_THREADS) adjoint_stage2_kernel(const grav_
 
 	double s[7] = {0, 0, 0, 0, 0, 0, 0};
 	if (flags & ADJ_STEP) {
-		// slots p, p + ATPR, ... added in order; each round issues all its loads first
-		// (the ones past the end are skipped), so a short list costs one latency
+		// slots p, p + ATPR, ... hold FP32 (hi, lo) pairs; they are added in order into
+		// compensated FP32 sums (hi by TwoSum, lo and the errors into l), each round
+		// issuing all its loads first (the ones past the end are skipped), combined
+		// across the lanes by a TwoSum butterfly and widened once: no FP64 arithmetic
+		// per slot (GB300 runs FP64 at ~1/64 of the FP32 rate)
 		constexpr int SLOT_BATCH = 4;
-		const double* part = b.part + static_cast<int64_t>(S.slot_base) * 7 * IT + li;
-		for (int k = p; k < S.nslots; k += SLOT_BATCH * ATPR) {
-			const int m = min(SLOT_BATCH, (S.nslots - k + ATPR - 1) / ATPR);
-			double q[SLOT_BATCH][7];
+		const int64_t stride = 7 * static_cast<int64_t>(IT);  // 8-byte entries per slot
+		// unique-pair plans: the last (row block index) slots of a segment are column
+		// slots holding FP32 values in their first half (adjoint_sym.cu)
+		const int nrow = b.mode == GRAV_MODE_FP32U ? S.nslots - S.il0 / IT : S.nslots;
+		const float2* part =
+			reinterpret_cast<const float2*>(b.part + static_cast<int64_t>(S.slot_base) * stride) + li;
+		float h[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, l[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+		for (int k = p; k < nrow; k += SLOT_BATCH * ATPR) {
+			const int m = min(SLOT_BATCH, (nrow - k + ATPR - 1) / ATPR);
+			float2 q[SLOT_BATCH][7];
 #pragma unroll
 			for (int j = 0; j < SLOT_BATCH; ++j)
 				if (j < m) {
 #pragma unroll
-					for (int c = 0; c < 7; ++c)
-						q[j][c] = __ldg(part + (static_cast<int64_t>(k + j * ATPR) * 7 + c) * IT);
+					for (int c = 0; c < 7; ++c) q[j][c] = __ldg(part + (k + j * ATPR) * stride + c * IT);
 				}
 #pragma unroll
 			for (int j = 0; j < SLOT_BATCH; ++j)
 				if (j < m) {
 #pragma unroll
-					for (int c = 0; c < 7; ++c) s[c] += q[j][c];
+					for (int c = 0; c < 7; ++c) {
+						two_sum_acc(h[c], l[c], q[j][c].x);
+						l[c] += q[j][c].y;
+					}
 				}
 		}
+		const float* cpart =
+			reinterpret_cast<const float*>(b.part + static_cast<int64_t>(S.slot_base) * stride) + li;
+		for (int k = nrow + p; k < S.nslots; k += SLOT_BATCH * ATPR) {
+			float q[SLOT_BATCH][7];
 #pragma unroll
-		for (int o = 1; o < ATPR; o <<= 1)
+			for (int j = 0; j < SLOT_BATCH; ++j)
 #pragma unroll
-			for (int c = 0; c < 7; ++c) s[c] += __shfl_xor_sync(gmask, s[c], o);
+				for (int c = 0; c < 7; ++c)  // loads past the end read as 0, added exactly
+					q[j][c] = (k + j * ATPR < S.nslots) ? __ldg(cpart + (k + j * ATPR) * 2 * stride + c * IT)
+					                                  : 0.f;
+#pragma unroll
+			for (int j = 0; j < SLOT_BATCH; ++j)
+#pragma unroll
+				for (int c = 0; c < 7; ++c) two_sum_acc(h[c], l[c], q[j][c]);
+		}
+#pragma unroll
+		for (int c = 0; c < 7; ++c) {
+			group_sum_pair<ATPR>(h[c], l[c], gmask);
+			s[c] = static_cast<double>(h[c]) + static_cast<double>(l[c]);
+		}
 	}
 	if (p != 0) return;
 
@@ -324,8 +356,9 @@ int check_adj(const grav_adjoint* a)
 	using grav::record_error;
 	if (!a || !a->b) return record_error(GRAV_E_ARG, "NULL adjoint or batch");
 	const grav_batch* b = a->b;
-	if (b->mode != GRAV_MODE_FP32)
-		return record_error(GRAV_E_ARG, "the adjoint runs on an FP32-mode batch (float4 positions)");
+	if (b->mode != GRAV_MODE_FP32 && b->mode != GRAV_MODE_FP32U)
+		return record_error(GRAV_E_ARG, "the adjoint runs on an FP32 (all pairs, grav_plan) or "
+			"FP32U (unique pairs, grav_plan_pairs) batch");
 	if (!b->univ || !b->seg || !b->pos || !b->r || !b->v || !b->err)
 		return record_error(GRAV_E_ARG, "NULL device pointer in grav_batch");
 	if (!a->gr || !a->gv || !a->ggm || !a->upos || !a->part7)
@@ -338,9 +371,14 @@ int check_adj(const grav_adjoint* a)
 
 }  // namespace
 
-extern "C" int grav_adjoint_tile_supported(const grav_tile* t)
+extern "C" int grav_adjoint_tile_supported(int mode, const grav_tile* t)
 {
 	if (!t) return 0;
+	if (mode == GRAV_MODE_FP32U) {
+		int occ = 0;
+		return grav::vjp_sym_occupancy(t->bpt, t->threads, t->jtile, &occ) != 0 ? 1 : 0;
+	}
+	if (mode != GRAV_MODE_FP32) return 0;
 	const grav::VjpKernel* tab = nullptr;
 	const int n = grav::vjp_table(&tab);
 	for (int i = 0; i < n; ++i)
@@ -348,9 +386,18 @@ extern "C" int grav_adjoint_tile_supported(const grav_tile* t)
 	return 0;
 }
 
-extern "C" int grav_adjoint_occupancy(const grav_tile* t, int32_t* ctas_per_sm)
+extern "C" int grav_adjoint_occupancy(int mode, const grav_tile* t, int32_t* ctas_per_sm)
 {
 	if (!t || !ctas_per_sm) return grav::record_error(GRAV_E_ARG, "NULL argument");
+	if (mode == GRAV_MODE_FP32U) {
+		int occ = 0;
+		const int rc = grav::vjp_sym_occupancy(t->bpt, t->threads, t->jtile, &occ);
+		if (rc == 0) return grav::record_error(GRAV_E_TILE, "tile shape has no unique-pair adjoint kernel");
+		if (rc < 0) return grav::record_error(GRAV_E_CUDA, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+		*ctas_per_sm = occ;
+		return GRAV_OK;
+	}
+	if (mode != GRAV_MODE_FP32) return grav::record_error(GRAV_E_ARG, "adjoint mode must be FP32 or FP32U");
 	const grav::VjpKernel* tab = nullptr;
 	const int n = grav::vjp_table(&tab);
 	for (int i = 0; i < n; ++i)
@@ -389,18 +436,25 @@ extern "C" int grav_adjoint_step(const grav_adjoint* a, void* stream)
 	if (b.n_units > 0) {
 		if (b.tile.grid <= 0 || b.tile.grid > b.n_units)
 			return grav::record_error(GRAV_E_ARG, "tile.grid must be in [1, n_units]");
-		const grav::VjpKernel* tab = nullptr;
-		const int n = grav::vjp_table(&tab);
-		const grav::VjpKernel* k = nullptr;
-		for (int i = 0; i < n; ++i)
-			if (tab[i].bpt == b.tile.bpt && tab[i].threads == b.tile.threads &&
-				tab[i].jtile == b.tile.jtile)
-				k = &tab[i];
-		if (!k) return grav::record_error(GRAV_E_TILE, "tile shape has no adjoint kernel");
 		const float4* up = static_cast<const float4*>(a->upos);
-		void* args[] = {&copy, &up};
-		cudaError_t e = grav::launch_dependent(k->fn, b.tile.grid, k->threads, k->smem, st, args);
-		if (e != cudaSuccess) return grav::record_error(GRAV_E_CUDA, cudaGetErrorString(e));
+		if (b.mode == GRAV_MODE_FP32U) {
+			const cudaError_t e = grav::launch_vjp_sym(copy, up, st);
+			if (e == cudaErrorInvalidValue)
+				return grav::record_error(GRAV_E_TILE, "tile shape has no unique-pair adjoint kernel");
+			if (e != cudaSuccess) return grav::record_error(GRAV_E_CUDA, cudaGetErrorString(e));
+		} else {
+			const grav::VjpKernel* tab = nullptr;
+			const int n = grav::vjp_table(&tab);
+			const grav::VjpKernel* k = nullptr;
+			for (int i = 0; i < n; ++i)
+				if (tab[i].bpt == b.tile.bpt && tab[i].threads == b.tile.threads &&
+					tab[i].jtile == b.tile.jtile)
+					k = &tab[i];
+			if (!k) return grav::record_error(GRAV_E_TILE, "tile shape has no adjoint kernel");
+			void* args[] = {&copy, &up};
+			const cudaError_t e = grav::launch_dependent(k->fn, b.tile.grid, k->threads, k->smem, st, args);
+			if (e != cudaSuccess) return grav::record_error(GRAV_E_CUDA, cudaGetErrorString(e));
+		}
 	}
 	cudaError_t e = grav::launch_adjoint_stage2(copy, *a, ADJ_STEP | ADJ_PREPARE, st);
 	return e == cudaSuccess ? GRAV_OK : grav::record_error(GRAV_E_CUDA, cudaGetErrorString(e));

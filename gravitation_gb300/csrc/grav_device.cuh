@@ -125,6 +125,25 @@ __device__ __forceinline__ void grid_dep_launch()
 	asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+// Combine the compensated FP32 sums (H, L) of the WIDTH lanes of an aligned lane group
+// by an xor butterfly: H by TwoSum, L and the rounding error added.  Every lane ends
+// with the same bits: TwoSum's error term is the exact rounding error of H_a + H_b in
+// either operand order, and FP32 addition commutes.
+template <int WIDTH>
+__device__ __forceinline__ void group_sum_pair(float& H, float& L, unsigned mask)
+{
+#pragma unroll
+	for (int o = 1; o < WIDTH; o <<= 1) {
+		const float hb = __shfl_xor_sync(mask, H, o);
+		const float lb = __shfl_xor_sync(mask, L, o);
+		const float s = H + hb;
+		const float bp = s - H;
+		const float e = (H - (s - bp)) + (hb - bp);
+		H = s;
+		L = (L + lb) + e;
+	}
+}
+
 // Record the first error code seen by any CTA.
 __device__ __forceinline__ void set_error(int* err, int code)
 {

@@ -161,14 +161,16 @@ __global__ void __launch_bounds__(T) stage1_f32_kernel(const grav_batch b)
 		}
 		if (timed_out) break;
 
-		// FP64 partial of this CTA's piece of the segment
+		// this CTA's piece of the segment: the compensated sums go out as FP32 (hi, lo)
+		// pairs, one 8-byte slot entry each, with no FP64 arithmetic (GB300 runs FP64 at
+		// ~1/64 of the FP32 rate); stage 2 adds the pairs in FP32 by TwoSum
 		const int64_t slot = S.slot_base + (c - S.cta_first);
-		double* __restrict__ out = b.part + slot * 3 * IT;
+		float2* __restrict__ out = reinterpret_cast<float2*>(b.part + slot * 3 * IT);
 #pragma unroll
 		for (int k = 0; k < B; ++k) {
-			out[tid + k * T] = static_cast<double>(hx[k]) + static_cast<double>(lx[k]);
-			out[IT + tid + k * T] = static_cast<double>(hy[k]) + static_cast<double>(ly[k]);
-			out[2 * IT + tid + k * T] = static_cast<double>(hz[k]) + static_cast<double>(lz[k]);
+			out[tid + k * T] = make_float2(hx[k], lx[k]);
+			out[IT + tid + k * T] = make_float2(hy[k], ly[k]);
+			out[2 * IT + tid + k * T] = make_float2(hz[k], lz[k]);
 		}
 		ub = S.unit_begin + jt1;
 		++s;

@@ -241,14 +241,15 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 		}
 		if (timed_out) break;
 
+		// row sums of this CTA's piece as FP32 (hi, lo) pairs, one 8-byte slot entry each
 		const int64_t slot = S.slot_base + (c - S.cta_first);
-		double* __restrict__ out = b.part + slot * 3 * R;
+		float2* __restrict__ out = reinterpret_cast<float2*>(b.part + slot * 3 * R);
 		const int r0 = warp * 32 * B + lane;
 #pragma unroll
 		for (int k = 0; k < B; ++k) {
-			out[r0 + k * 32] = static_cast<double>(hx[k]) + static_cast<double>(lx[k]);
-			out[R + r0 + k * 32] = static_cast<double>(hy[k]) + static_cast<double>(ly[k]);
-			out[2 * R + r0 + k * 32] = static_cast<double>(hz[k]) + static_cast<double>(lz[k]);
+			out[r0 + k * 32] = make_float2(hx[k], lx[k]);
+			out[R + r0 + k * 32] = make_float2(hy[k], ly[k]);
+			out[2 * R + r0 + k * 32] = make_float2(hz[k], lz[k]);
 		}
 		ub = S.unit_begin + t1;
 		++s;

@@ -19,9 +19,8 @@ struct __align__(32) drow4 {
 // Lanes per row: for small batches the row's slots are split over TPR adjacent lanes
 // of a warp (lane p takes slots p, p + TPR, ...), so a few dozen slots cost one round
 // of memory latency, and the lanes' partial sums are combined by a butterfly, which
-// gives every lane the same bits (each addition pairs the same two operands on both
-// sides).  For large batches one lane per row: the extra lanes' FP64 combining adds
-// and conversions would run on GB300's FP64 pipe (~1/64 of the FP32 rate).
+// gives every lane the same bits.  For large batches one lane per row: there the extra
+// lanes and their combining work cost more than the latency they hide.
 constexpr int S2_THREADS = 128;
 constexpr int SPLIT_ROWS_MAX = 32768;  // TPR = 4 up to this many padded rows, else 1
 constexpr int ROW_BATCH = 8;           // FP64 row-slot loads in flight per lane
@@ -75,72 +74,107 @@ __global__ void __launch_bounds__(S2_THREADS) stage2_kernel(const grav_batch b, 
 
 	double ax = 0.0, ay = 0.0, az = 0.0;
 	if (!(flags & GRAV_S2_PREPARE)) {
-		const int64_t stride = 3 * static_cast<int64_t>(IT);
-		const double* __restrict__ part = b.part + static_cast<int64_t>(S.slot_base) * stride + li;
+		const int64_t stride = 3 * static_cast<int64_t>(IT);  // 8-byte entries per slot
 		// unique-pair plans: the last (row block index) slots of a segment are column
 		// slots holding FP32 sums in their first half (stage1_sym.cu)
 		const bool pairs = b.mode == GRAV_MODE_FP32U || b.mode == GRAV_MODE_FP32CU;
 		const int nrow = pairs ? S.nslots - S.il0 / IT : S.nslots;
-		// FP64 row slots p, p + TPR, ... added in order; each round issues all its loads
-		// first (the ones past the end are skipped), so a short list costs one latency
-		for (int k = p; k < nrow; k += ROW_BATCH * TPR) {
-			const int m = min(ROW_BATCH, (nrow - k + TPR - 1) / TPR);
-			double px[ROW_BATCH], py[ROW_BATCH], pz[ROW_BATCH];
+		if (b.mode == GRAV_MODE_FP64) {
+			// FP64 row slots p, p + TPR, ... added in order; each round issues all its
+			// loads first (the ones past the end are skipped): one latency per round
+			const double* __restrict__ part =
+				b.part + static_cast<int64_t>(S.slot_base) * stride + li;
+			for (int k = p; k < nrow; k += ROW_BATCH * TPR) {
+				const int m = min(ROW_BATCH, (nrow - k + TPR - 1) / TPR);
+				double px[ROW_BATCH], py[ROW_BATCH], pz[ROW_BATCH];
 #pragma unroll
-			for (int q = 0; q < ROW_BATCH; ++q) {
-				if (q < m) {
-					const double* ps = part + (k + q * TPR) * stride;
-					px[q] = __ldg(ps);
-					py[q] = __ldg(ps + IT);
-					pz[q] = __ldg(ps + 2 * IT);
-				}
-			}
-#pragma unroll
-			for (int q = 0; q < ROW_BATCH; ++q) {
-				if (q < m) {
-					ax += px[q];
-					ay += py[q];
-					az += pz[q];
-				}
-			}
-		}
-		if (pairs) {
-			// FP32 column slots: added by TwoSum in FP32 (hi + lo, ~48 bits) and widened
-			// once; FP64 adds per slot would run on GB300's FP64 pipe.  Loads past the end
-			// read as 0, which TwoSum adds exactly
-			const float* __restrict__ cpart =
-				reinterpret_cast<const float*>(b.part + static_cast<int64_t>(S.slot_base) * stride) + li;
-			const int64_t fstride = 2 * stride;  // floats per slot
-			float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
-			for (int k = nrow + p; k < S.nslots; k += COL_BATCH * TPR) {
-				float px[COL_BATCH], py[COL_BATCH], pz[COL_BATCH];
-#pragma unroll
-				for (int q = 0; q < COL_BATCH; ++q) {
-					px[q] = py[q] = pz[q] = 0.f;
-					if (k + q * TPR < S.nslots) {
-						const float* ps = cpart + (k + q * TPR) * fstride;
+				for (int q = 0; q < ROW_BATCH; ++q) {
+					if (q < m) {
+						const double* ps = part + (k + q * TPR) * stride;
 						px[q] = __ldg(ps);
 						py[q] = __ldg(ps + IT);
 						pz[q] = __ldg(ps + 2 * IT);
 					}
 				}
 #pragma unroll
-				for (int q = 0; q < COL_BATCH; ++q) {
-					two_sum_acc(hx, lx, px[q]);
-					two_sum_acc(hy, ly, py[q]);
-					two_sum_acc(hz, lz, pz[q]);
+				for (int q = 0; q < ROW_BATCH; ++q) {
+					if (q < m) {
+						ax += px[q];
+						ay += py[q];
+						az += pz[q];
+					}
 				}
 			}
-			ax += static_cast<double>(hx) + static_cast<double>(lx);
-			ay += static_cast<double>(hy) + static_cast<double>(ly);
-			az += static_cast<double>(hz) + static_cast<double>(lz);
-		}
-		// combine the lanes' sums: ((s0 + s1) + (s2 + s3)) on every lane
 #pragma unroll
-		for (int o = 1; o < TPR; o <<= 1) {
-			ax += __shfl_xor_sync(gmask, ax, o);
-			ay += __shfl_xor_sync(gmask, ay, o);
-			az += __shfl_xor_sync(gmask, az, o);
+			for (int o = 1; o < TPR; o <<= 1) {
+				ax += __shfl_xor_sync(gmask, ax, o);
+				ay += __shfl_xor_sync(gmask, ay, o);
+				az += __shfl_xor_sync(gmask, az, o);
+			}
+		} else {
+			// FP32 modes: row slots hold the stage-1 pieces' compensated sums as FP32
+			// (hi, lo) pairs; they and the column slots are added in slot order into a
+			// compensated FP32 sum (hi by TwoSum, lo and the errors into L), combined
+			// across the lanes by a TwoSum butterfly, and widened once.  No FP64
+			// arithmetic per slot: GB300 runs FP64 at ~1/64 of the FP32 rate
+			float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
+			const float2* __restrict__ rpart =
+				reinterpret_cast<const float2*>(b.part + static_cast<int64_t>(S.slot_base) * stride) + li;
+			for (int k = p; k < nrow; k += ROW_BATCH * TPR) {
+				const int m = min(ROW_BATCH, (nrow - k + TPR - 1) / TPR);
+				float2 px[ROW_BATCH], py[ROW_BATCH], pz[ROW_BATCH];
+#pragma unroll
+				for (int q = 0; q < ROW_BATCH; ++q) {
+					if (q < m) {
+						const float2* ps = rpart + (k + q * TPR) * stride;
+						px[q] = __ldg(ps);
+						py[q] = __ldg(ps + IT);
+						pz[q] = __ldg(ps + 2 * IT);
+					}
+				}
+#pragma unroll
+				for (int q = 0; q < ROW_BATCH; ++q) {
+					if (q < m) {
+						two_sum_acc(hx, lx, px[q].x);
+						two_sum_acc(hy, ly, py[q].x);
+						two_sum_acc(hz, lz, pz[q].x);
+						lx += px[q].y;
+						ly += py[q].y;
+						lz += pz[q].y;
+					}
+				}
+			}
+			if (pairs) {
+				// FP32 column slots; loads past the end read as 0, which TwoSum adds exactly
+				const float* __restrict__ cpart = reinterpret_cast<const float*>(
+					b.part + static_cast<int64_t>(S.slot_base) * stride) + li;
+				const int64_t fstride = 2 * stride;  // floats per slot
+				for (int k = nrow + p; k < S.nslots; k += COL_BATCH * TPR) {
+					float px[COL_BATCH], py[COL_BATCH], pz[COL_BATCH];
+#pragma unroll
+					for (int q = 0; q < COL_BATCH; ++q) {
+						px[q] = py[q] = pz[q] = 0.f;
+						if (k + q * TPR < S.nslots) {
+							const float* ps = cpart + (k + q * TPR) * fstride;
+							px[q] = __ldg(ps);
+							py[q] = __ldg(ps + IT);
+							pz[q] = __ldg(ps + 2 * IT);
+						}
+					}
+#pragma unroll
+					for (int q = 0; q < COL_BATCH; ++q) {
+						two_sum_acc(hx, lx, px[q]);
+						two_sum_acc(hy, ly, py[q]);
+						two_sum_acc(hz, lz, pz[q]);
+					}
+				}
+			}
+			group_sum_pair<TPR>(hx, lx, gmask);
+			group_sum_pair<TPR>(hy, ly, gmask);
+			group_sum_pair<TPR>(hz, lz, gmask);
+			ax = static_cast<double>(hx) + static_cast<double>(lx);
+			ay = static_cast<double>(hy) + static_cast<double>(ly);
+			az = static_cast<double>(hz) + static_cast<double>(lz);
 		}
 	}
 	if (p != 0) return;

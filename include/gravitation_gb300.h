@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define GRAV_ABI_VERSION 1
+#define GRAV_ABI_VERSION 2
 
 /* status codes */
 #define GRAV_OK 0
@@ -47,7 +47,7 @@ extern "C" {
 #define GRAV_DEV_TIMEOUT 1    /* a bounded wait for a bulk copy expired */
 
 /* precision modes (universe_base dtype / kernel meta "precision") */
-#define GRAV_MODE_FP32 0      /* FP32 separations and weights, FP32 tile partials summed in FP64 */
+#define GRAV_MODE_FP32 0      /* FP32 separations and weights, compensated FP32 (hi + lo) sums */
 #define GRAV_MODE_FP32C 1     /* as FP32 with double-single (hi+lo) positions: separations exact */
 #define GRAV_MODE_FP64 2      /* FP64 throughout */
 #define GRAV_MODE_FP32U 3     /* FP32 arithmetic of GRAV_MODE_FP32 on unique pairs (each pair
@@ -76,8 +76,8 @@ typedef struct grav_seg_desc {
 	int32_t il0;        /* first local body of the i-tile */
 	int32_t n_units;    /* j-tiles to visit (0 for a tile made only of padding) */
 	int32_t cta_first;  /* first CTA of the persistent grid that works on it */
-	int32_t slot_base;  /* first FP64 partial-sum slot of this segment */
-	int32_t nslots;     /* number of CTAs that work on it (= slots) */
+	int32_t slot_base;  /* first partial-sum slot of this segment */
+	int32_t nslots;     /* its slots: one per CTA that works on it (+ column slots, pair plans) */
 } grav_seg_desc;
 
 /* Tile shape of the stage-1 kernel. */
@@ -95,7 +95,7 @@ typedef struct grav_plan_info {
 	int64_t n_units;     /* total work units (i-tile x j-tile) */
 	int32_t n_univ;
 	int32_t n_seg;       /* = n_pad_total / itile */
-	int32_t n_slots;     /* FP64 partial-sum slots (each 3 x itile doubles) */
+	int32_t n_slots;     /* partial-sum slots (each 3 x itile 8-byte entries) */
 	int32_t itile;       /* bpt * threads */
 	int32_t pad_unit;    /* max(itile, jtile) */
 	int32_t grid;        /* CTAs actually launched */
@@ -224,9 +224,11 @@ int grav_energy(const grav_batch* b, double* out, void* stream);
 
 /* ---- adjoint (reverse-mode gradients) -------------------------------------------------- */
 
-/* Buffers of the backward sweep.  `b` is an FP32-mode batch planned with an adjoint
- * tile (grav_adjoint_tile_supported); b->r, b->v hold the state being reversed (start:
- * the state after the last forward step of the segment), b->pos is scratch. */
+/* Buffers of the backward sweep.  `b` is a batch planned with an adjoint tile
+ * (grav_adjoint_tile_supported): mode GRAV_MODE_FP32 with grav_plan (every ordered pair)
+ * or GRAV_MODE_FP32U with grav_plan_pairs (each unordered pair once); b->r, b->v hold
+ * the state being reversed (start: the state after the last forward step of the
+ * segment), b->pos is scratch. */
 typedef struct grav_adjoint {
 	const grav_batch* b;
 	double* gr;    /* n_bodies x 4: dL/dr of the current state (in/out) */
@@ -236,11 +238,13 @@ typedef struct grav_adjoint {
 	double* part7; /* n_slots x 7 x itile doubles: scratch */
 } grav_adjoint;
 
-/* 1 if `tile` has a compiled adjoint pair kernel. */
-int grav_adjoint_tile_supported(const grav_tile* tile);
+/* 1 if `tile` has a compiled adjoint pair kernel for `mode` (GRAV_MODE_FP32: all
+ * ordered pairs; GRAV_MODE_FP32U: unique pairs). */
+int grav_adjoint_tile_supported(int mode, const grav_tile* tile);
 
-/* Resident CTAs per SM of the adjoint pair kernel for `tile` on the current device. */
-int grav_adjoint_occupancy(const grav_tile* tile, int32_t* ctas_per_sm);
+/* Resident CTAs per SM of the adjoint pair kernel for `mode` and `tile` on the current
+ * device. */
+int grav_adjoint_occupancy(int mode, const grav_tile* tile, int32_t* ctas_per_sm);
 
 /* Start of a backward segment: from b->r, b->v (state k+1) and gr, gv, write the FP32
  * positions r_k = r_{k+1} - T v_{k+1} and u = gv + T gr used by the next step. */

@@ -35,12 +35,16 @@ def relerr(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
-def test_single_step_against_oracle_vjp(gpu):
+@pytest.mark.parametrize('pairs', [False, True])
+def test_single_step_against_oracle_vjp(gpu, pairs):
+    """Both backward pair kernels: every ordered pair, and each unordered pair once
+    (700 bodies = 3 row blocks of the unique-pair plan, so column slots are used)."""
     n = 700
     r, v, m = compact(n, 3)
     rng = np.random.default_rng(1)
     c = rng.normal(size=(n, 3))
-    ro = Rollout([n], T, 1, every=1)
+    ro = Rollout([n], T, 1, every=1, adj_pairs=pairs)
+    assert ro.adj.pairs == pairs
     dev = torch.device('cuda')
     rK, vK = ro.forward(torch.tensor(r, device=dev), torch.tensor(v, device=dev),
                         torch.tensor(G_DEFAULT * m, device=dev))
@@ -59,9 +63,10 @@ def test_single_step_against_oracle_vjp(gpu):
     assert np.max(np.abs(v_rev.cpu().numpy() - v)) <= 1e-15 + 1e-9 * np.max(np.abs(v))
 
 
-@pytest.mark.parametrize('every', [1, 8, 40])
-def test_rollout_against_torch_autograd(gpu, every):
-    n, steps = 192, 40
+@pytest.mark.parametrize('every,n,pairs', [(1, 192, None), (8, 192, None), (40, 192, None),
+                                           (8, 600, True)])
+def test_rollout_against_torch_autograd(gpu, every, n, pairs):
+    steps = 40
     r, v, m = compact(n, 5)
     tgt = r + np.random.default_rng(2).normal(scale=1.0, size=r.shape)
     dev = torch.device('cuda')
@@ -76,7 +81,8 @@ def test_rollout_against_torch_autograd(gpu, every):
         loss.backward()
         return [x.grad.cpu().numpy() for x in (r0, v0, mm)], float(loss)
 
-    ours, l1 = grads(lambda a, b, c: rollout(a, b, c, G, T, steps, every=every))
+    ro = Rollout([n], T, steps, every, adj_pairs=pairs) if pairs is not None else None
+    ours, l1 = grads(lambda a, b, c: rollout(a, b, c, G, T, steps, every=every, ro=ro))
     ref, l2 = grads(lambda a, b, c: torch_reference_rollout(a, b, c, G, T, steps))
     assert abs(l1 - l2) <= 1e-6 * abs(l2)
     for name, x, y in zip(('r0', 'v0', 'm'), ours, ref):
