@@ -23,11 +23,11 @@ ADJ_TILE = (2, 128, 128)
 
 
 def default_adjoint_pairs(sizes):
-    """The unique-pair backward kernel from ~6k bodies (4e7 ordered pairs) on.  Measured
-    on GB300, backward step (graph-replayed) all pairs vs unique pairs: N = 4096 --
-    32.8 vs 32.4 us (no gain: the unique-pair units are too coarse there), N = 8192 --
-    117 vs 95 us, N = 16384 -- 385 vs 313 us, N = 65536 -- 5.63 vs 4.15 ms."""
-    return sum(int(n) * int(n) for n in sizes) >= 40_000_000
+    """The unique-pair backward kernel from ~4k bodies (1.6e7 ordered pairs) on.
+    Measured on GB300, backward step (graph-replayed), all pairs vs unique pairs:
+    N = 4096 -- 32.5 vs 31.2 us (8 warps, 2 rows/thread, 64-body j-tiles), N = 8192 --
+    116 vs 94 us, N = 16384 -- 385 vs 313 us, N = 65536 -- 5.63 vs 4.15 ms."""
+    return sum(int(n) * int(n) for n in sizes) >= 16_000_000
 
 
 def default_adjoint_tile(sizes, pairs=False):
@@ -38,8 +38,12 @@ def default_adjoint_tile(sizes, pairs=False):
     (1, 64, 128) / (2, 64, 128) / (1, 128, 64) / (2, 64, 64); N = 65536 -- 5.16 ms with
     (2, 128, 128), 5.62 ms with (1, 128, 128)."""
     if pairs:
-        # unique pairs: 2 rows/thread and 64-body j-tiles up to ~20k bodies, 4 and 128 above
-        return (2, 128, 64) if sum(int(n) * int(n) for n in sizes) <= 400_000_000 else (4, 128, 128)
+        # unique pairs: 2 rows/thread and 64-body j-tiles (8 warps up to ~6k bodies, 4
+        # warps up to ~20k), 4 rows/thread and 128-body j-tiles above
+        n2 = sum(int(n) * int(n) for n in sizes)
+        if n2 < 40_000_000:
+            return (2, 256, 64)
+        return (2, 128, 64) if n2 <= 400_000_000 else (4, 128, 128)
     if sum(int(n) * int(n) for n in sizes) <= 100_000_000:
         return (1, 128, 128)
     return ADJ_TILE
@@ -50,7 +54,8 @@ class AdjointEngine:
 
     pairs: True -- the unique-pair backward kernel (each unordered pair once, plan of
     grav_plan_pairs); False -- every ordered pair (plan of grav_plan); None -- by size.
-    tile: (bpt, threads, jtile) of that kernel, default by size."""
+    tile: (bpt, threads, jtile) of that kernel, default by size, optionally with a fourth
+    entry, the persistent grid (default: SMs x resident CTAs)."""
 
     def __init__(self, sizes, T, device=None, tile=None, pairs=None):
         self.lib = _lib.load()
@@ -71,6 +76,8 @@ class AdjointEngine:
         with torch.cuda.device(self.device):
             check(self.lib.grav_adjoint_occupancy(mode, ctypes.byref(t), ctypes.byref(occ)))
         t.grid = self.dev_info.sm_count * max(occ.value, 1)
+        if len(tile) > 3 and tile[3]:
+            t.grid = max(1, int(tile[3]))
         self.info, univ, seg = make_plan(self.sizes, T, t, 'fp32u' if self.pairs else 'fp32')
         info, dev = self.info, self.device
         self.univ_dev = _ctypes_to_device(univ, ctypes.sizeof(_lib.UnivDesc) * info.n_univ, dev)

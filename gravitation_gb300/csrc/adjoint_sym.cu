@@ -297,6 +297,7 @@ struct VjpSymKernel {
 	{B, 32 * W, J, reinterpret_cast<const void*>(&vjp_sym_kernel<B, W, J>), 2 * 2 * J * 16}
 
 static const VjpSymKernel k_vjp_sym[] = {
+	GRAV_VJPSYM_ENTRY(2, 8, 64),
 	GRAV_VJPSYM_ENTRY(2, 4, 64),
 	GRAV_VJPSYM_ENTRY(4, 4, 128),
 };
