@@ -50,7 +50,7 @@ L2_FLUSH_BYTES = 256 << 20
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
-    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--steps', type=int, default=200)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', choices=('ours', 'reference'), default='ours')
     ap.add_argument('--n', type=int, default=65536)
@@ -124,15 +124,20 @@ def allreduce_max(x, world, device):
 # ---- clocks ---------------------------------------------------------------------------------
 
 class ClockSampler:
-    """nvidia-smi sampling of SM clock and throttle reasons during the timed region."""
-    FIELDS = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+    """nvidia-smi sampling (every 100 ms) of SM clock, power and throttle reasons.
+    Samples are time-stamped; the summary keeps those taken inside the window that
+    mark()/unmark() bracket (the timed region), and falls back to every sample only
+    when the window is shorter than the sampling period."""
+    FIELDS = ('timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
               'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
               'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+    PERIOD_MS = 100
 
     def __init__(self, index):
         self.index = index
         self.proc = None
         self.path = None
+        self.window = [None, None]
 
     def start(self):
         fd, self.path = tempfile.mkstemp(suffix='.csv')
@@ -140,11 +145,25 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ['nvidia-smi', '-i', str(self.index), '--query-gpu=' + self.FIELDS,
-                 '--format=csv,noheader,nounits', '-lms', '200'],
+                 '--format=csv,noheader,nounits', '-lms', str(self.PERIOD_MS)],
                 stdout=open(self.path, 'w'), stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
         time.sleep(0.3)
+
+    def mark(self):
+        self.window[0] = time.time()
+
+    def unmark(self):
+        self.window[1] = time.time()
+
+    @staticmethod
+    def _epoch(stamp):
+        import datetime
+        try:
+            return datetime.datetime.strptime(stamp, '%Y/%m/%d %H:%M:%S.%f').timestamp()
+        except ValueError:
+            return None
 
     def stop(self):
         if self.proc is None:
@@ -155,27 +174,35 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        sm, smax, power, reasons = [], [], [], set()
+        rows = []
         names = ('hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap')
         with open(self.path) as f:
             for line in f:
                 p = [x.strip() for x in line.split(',')]
-                if len(p) < 9:
+                if len(p) < 10:
                     continue
                 try:
-                    sm.append(float(p[1]))
-                    smax.append(float(p[2]))
-                    power.append(float(p[3]))
+                    vals = (float(p[2]), float(p[3]), float(p[4]))
                 except ValueError:
                     continue
-                for nm, val in zip(names, p[5:9]):
-                    if val.lower() == 'active':
-                        reasons.add(nm)
+                active = {nm for nm, val in zip(names, p[6:10]) if val.lower() == 'active'}
+                rows.append((self._epoch(p[0]), vals, active))
         os.unlink(self.path)
-        if not sm:
+        t0, t1 = self.window
+        inside = [x for x in rows if x[0] is not None and t0 is not None and t1 is not None
+                  and t0 <= x[0] <= t1]
+        scope = 'timed region'
+        if not inside:
+            inside, scope = rows, 'whole run (timed region shorter than the sampling period)'
+        if not inside:
             return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['no samples']}
-        return {'sm_mhz': statistics.median(sm), 'sm_max_mhz': max(smax),
-                'power_w_max': max(power), 'samples': len(sm), 'reasons': sorted(reasons)}
+        sm = [x[1][0] for x in inside]
+        reasons = set().union(*[x[2] for x in inside])
+        return {'sm_mhz': statistics.median(sm), 'sm_mhz_min': min(sm),
+                'sm_max_mhz': max(x[1][1] for x in inside),
+                'power_w_max': max(x[1][2] for x in inside), 'samples': len(sm),
+                'samples_scope': scope, 'period_ms': self.PERIOD_MS,
+                'reasons': sorted(reasons)}
 
 
 def workload_name(n, mode):
@@ -349,6 +376,7 @@ def run_ours(args):
            for _ in range(args.steps)]
     barrier(world)
     torch.cuda.synchronize()
+    clocks.mark()
     t_wall0 = time.perf_counter()
     for k in range(args.steps):
         flush.zero_()
@@ -370,6 +398,7 @@ def run_ours(args):
         eng.stage1()
         s1[k][1].record(stream)
     torch.cuda.synchronize()
+    clocks.unmark()
     clk = clocks.stop()
     s1_ms = [a.elapsed_time(b) for a, b in s1]
     peak = measure_fp32_peak(torch, lib, info, device)

@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, 'libgravgb300.so')
 
 # ---- constants (mirror of the header) -------------------------------------------
-GRAV_ABI_VERSION = 2
+GRAV_ABI_VERSION = 3
 GRAV_OK = 0
 GRAV_E_ARG = -1
 GRAV_E_TILE = -2
@@ -88,7 +88,8 @@ class Batch(ctypes.Structure):
 
 class Adjoint(ctypes.Structure):
     _fields_ = [('b', ctypes.POINTER(Batch)), ('gr', ctypes.c_void_p), ('gv', ctypes.c_void_p),
-                ('ggm', ctypes.c_void_p), ('upos', ctypes.c_void_p), ('part7', ctypes.c_void_p)]
+                ('ggm', ctypes.c_void_p), ('upos', ctypes.c_void_p), ('part7', ctypes.c_void_p),
+                ('a_in', ctypes.c_void_p)]
 
 
 GRAV_SCEN_UNIFORM_CUBE = 1

@@ -3,11 +3,13 @@
 ``rollout(r0, v0, m, G, T, steps, every)`` is a torch.autograd.Function: its forward
 runs ``steps`` GB300 steps (FP32 stage 1, FP64 stage 2) and keeps the FP64 state at
 the start of every ``every``-step segment; its backward sweeps the segments from last
-to first.  Each segment starts from the exact stored state at its end, reverses the
-update step by step in FP64 while the adjoint pair kernel recomputes stage 1 at each
-reconstructed position and applies the transposed stage 2 and stage 1 (see
-csrc/adjoint.cu).  Gradients are returned for the initial positions, velocities and
-masses.  Memory: one FP64 state per segment, no per-step storage.
+to first.  Each segment starts from the exact stored state at its end and reverses the
+update step by step in FP64, while the adjoint pair kernel applies the transposed
+stage 2 and stage 1 at each reconstructed position (see csrc/adjoint.cu).  The
+reversal uses the forward's own accelerations of each step where they are kept
+(``store_a``: steps x 32 bytes per body), else the pair kernel recomputes stage 1 as
+well.  Gradients are returned for the initial positions, velocities and masses.
+Memory: one FP64 state per segment, plus the kept accelerations.
 """
 
 import ctypes
@@ -22,12 +24,18 @@ from .engine import Engine, device_info, make_plan, _ctypes_to_device
 ADJ_TILE = (2, 128, 128)
 
 
-def default_adjoint_pairs(sizes):
+def default_adjoint_pairs(sizes, budget=None):
     """The unique-pair backward kernel from ~4k bodies (1.6e7 ordered pairs) on.
     Measured on GB300, backward step (graph-replayed), all pairs vs unique pairs:
     N = 4096 -- 32.5 vs 31.2 us (8 warps, 2 rows/thread, 64-body j-tiles), N = 8192 --
-    116 vs 94 us, N = 16384 -- 385 vs 313 us, N = 65536 -- 5.63 vs 4.15 ms."""
-    return sum(int(n) * int(n) for n in sizes) >= 16_000_000
+    116 vs 94 us, N = 16384 -- 385 vs 313 us, N = 65536 -- 5.63 vs 4.15 ms.
+    Above the slot budget (engine.slot_budget_bytes, or `budget` bytes) the all-pairs
+    kernel is used: the unique-pair plan keeps 7-component slots per pair of row blocks."""
+    if sum(int(n) * int(n) for n in sizes) < 16_000_000:
+        return False
+    from .engine import pair_plan_fits
+    t = default_adjoint_tile(sizes, True)
+    return pair_plan_fits(sizes, budget, comps=7, tiles=[_lib.Tile(t[0], t[1], t[2], 1)])
 
 
 def default_adjoint_tile(sizes, pairs=False):
@@ -107,6 +115,7 @@ class AdjointEngine:
         a.b = ctypes.pointer(b)
         a.gr, a.gv, a.ggm = self.gr.data_ptr(), self.gv.data_ptr(), self.ggm.data_ptr()
         a.upos, a.part7 = self.upos.data_ptr(), self.part7.data_ptr()
+        a.a_in = None
         self.adj = a
         self._aref = ctypes.byref(a)
 
@@ -122,8 +131,15 @@ class AdjointEngine:
     def prepare(self, stream=None):
         check(self.lib.grav_adjoint_prepare(self._aref, self._h(stream)))
 
-    def step(self, stream=None):
-        check(self.lib.grav_adjoint_step(self._aref, self._h(stream)))
+    def step(self, stream=None, a_in=None):
+        """One backward step.  a_in: the forward's accelerations of the step being
+        reversed (float64 [n_bodies, 4] device tensor, as stage 2 wrote them with
+        GRAV_S2_WRITE_A); None lets the pair kernel recompute them."""
+        self.adj.a_in = None if a_in is None else a_in.data_ptr()
+        try:
+            check(self.lib.grav_adjoint_step(self._aref, self._h(stream)))
+        finally:
+            self.adj.a_in = None
 
     def raise_on_device_error(self):
         code = int(self.err.item())
@@ -133,19 +149,28 @@ class AdjointEngine:
 
 
 class Rollout:
-    """Forward engine + adjoint engine for one batch of universes (reusable)."""
+    """Forward engine + adjoint engine for one batch of universes (reusable).
+
+    store_a: keep the forward's FP64 accelerations of every step (steps x n_bodies x 32
+    bytes) so that the backward pair kernel forms only J^T u and the mass term instead
+    of recomputing stage 1 as well (about 15 % fewer operations per pair, 4 slot
+    components instead of 7), and the reversal v_k = v_{k+1} - T a_k uses the very a_k
+    of the forward.  None: when that fits the slot budget (engine.slot_budget_bytes)."""
 
     def __init__(self, sizes, T, steps, every=32, device=None, fwd_tile=None, tuner=None,
-                 mode=None, graphs=True, adj_pairs=None):
+                 mode=None, graphs=True, adj_pairs=None, store_a=None):
         self.sizes = [int(n) for n in sizes]
         self.T = float(T)
         self.steps = int(steps)
         self.every = max(1, int(every))
         if mode is None:
             # the forward's FP32 kernel by size, as the plugin picks it: all pairs for
-            # small universes, unique pairs from 8192 bodies
-            from .plugin import default_mode
-            mode = default_mode('float32', max(self.sizes))
+            # small universes, unique pairs from 8192 bodies while the batch's slots fit
+            from .plugin import UNIQUE_PAIRS_FROM_N
+            from .engine import pair_plan_fits
+            mode = 'fp32'
+            if max(self.sizes, default=0) >= UNIQUE_PAIRS_FROM_N and pair_plan_fits(self.sizes):
+                mode = 'fp32u'
         self.fwd = Engine(self.sizes, self.T, mode=mode, tile=fwd_tile, device=device,
                           tuner=tuner)
         self.adj = AdjointEngine(self.sizes, self.T, device=device, pairs=adj_pairs)
@@ -158,71 +183,105 @@ class Rollout:
         self.ck_r = torch.zeros((nseg + 1, n, 4), dtype=torch.float64, device=self.fwd.device)
         self.ck_v = torch.zeros_like(self.ck_r)
         self.checkpoints = []
+        if store_a is None:
+            from .engine import slot_budget_bytes
+            store_a = self.steps * max(n, 1) * 32 <= slot_budget_bytes(self.fwd.device)
+        self.store_a = bool(store_a)
+        # accelerations of every forward step (rows ax, ay, az, 0), written by stage 2
+        self.acc = (torch.zeros((max(self.steps, 1), max(n, 1), 4), dtype=torch.float64,
+                                device=self.fwd.device) if self.store_a else None)
 
     def _segments(self):
         starts = list(range(0, self.steps, self.every))
         return [(s, min(s + self.every, self.steps)) for s in starts]
 
-    def _fwd_steps(self, c, stream):
-        if not self.graphs:
-            self.fwd.step(c, stream=stream)
+    def _fwd_launch(self, s0, s1, stream):
+        """Forward steps s0 .. s1-1; with store_a each writes its accelerations to acc[k]
+        (the batch's a_out is pointed there for that launch and restored after)."""
+        f = self.fwd
+        if not self.store_a:
+            f.step(s1 - s0, stream=stream)
             return
-        g = self._fwd_graphs.get(c)
-        if g is None:
-            g = self._fwd_graphs[c] = self.fwd.capture_graph(c)
-        g.replay()
+        flags = _lib.GRAV_S2_INTEGRATE | _lib.GRAV_S2_WRITE_A
+        h = f._h(stream)
+        keep = f.batch.a_out
+        try:
+            for k in range(s0, s1):
+                f.batch.a_out = self.acc[k].data_ptr()
+                check(f.lib.grav_step(f._bref, flags, h))
+        finally:
+            f.batch.a_out = keep
 
-    def _adj_steps(self, c, stream):
-        a = self.adj
-        if not self.graphs:
-            for _ in range(c):
-                a.step(stream)
-            return
-        g = self._adj_graphs.get(c)
+    def _graph(self, cache, key, device, enqueue):
+        g = cache.get(key)
         if g is None:
-            side = torch.cuda.Stream(device=a.device)
-            side.wait_stream(torch.cuda.current_stream(a.device))
+            side = torch.cuda.Stream(device=device)
+            side.wait_stream(torch.cuda.current_stream(device))
             g = torch.cuda.CUDAGraph()
             with torch.cuda.graph(g, stream=side):
-                for _ in range(c):
-                    a.step(side)
-            torch.cuda.current_stream(a.device).wait_stream(side)
-            self._adj_graphs[c] = g
-        g.replay()
+                enqueue(side)
+            torch.cuda.current_stream(device).wait_stream(side)
+            cache[key] = g
+        return g
+
+    def _fwd_segment(self, si, s0, s1, stream):
+        """Checkpoint the state at the segment's start, then run its steps."""
+        n = self.fwd.info.n_bodies
+        with torch.cuda.stream(self.fwd._stream(stream)):
+            self.ck_r[si].copy_(self.fwd.r[:n])
+            self.ck_v[si].copy_(self.fwd.v[:n])
+        self._fwd_launch(s0, s1, stream)
+
+    def _adj_segment(self, si, s0, s1, stream):
+        """From the stored state at the segment's end, backward steps s1-1 down to s0."""
+        a = self.adj
+        with torch.cuda.stream(self.fwd._stream(stream)):
+            a.set_state(self.ck_r[si + 1], self.ck_v[si + 1])
+        a.prepare(stream)
+        for k in reversed(range(s0, s1)):
+            a.step(stream, a_in=self.acc[k] if self.store_a else None)
 
     def forward(self, r0, v0, gm, stream=None):
         """Run the steps; keep the FP64 state at the start of every segment.
         Returns device views (r[n,3], v[n,3]) of the final state.  With graphs=True each
-        segment's steps replay from a CUDA graph (captured on first use)."""
+        segment (its checkpoint copy and steps) replays from a CUDA graph captured on
+        first use."""
         n = self.fwd.info.n_bodies
         self.fwd.set_state(r0, v0, gm, stream=stream)
         segs = self._segments()
         for si, (s0, s1) in enumerate(segs):
-            self.ck_r[si].copy_(self.fwd.r[:n])
-            self.ck_v[si].copy_(self.fwd.v[:n])
-            self._fwd_steps(s1 - s0, stream)
-        self.ck_r[len(segs)].copy_(self.fwd.r[:n])
-        self.ck_v[len(segs)].copy_(self.fwd.v[:n])
+            if self.graphs:
+                self._graph(self._fwd_graphs, si, self.fwd.device,
+                            lambda st, a=si, b=s0, c=s1: self._fwd_segment(a, b, c, st)).replay()
+            else:
+                self._fwd_segment(si, s0, s1, stream)
+        with torch.cuda.stream(self.fwd._stream(stream)):
+            self.ck_r[len(segs)].copy_(self.fwd.r[:n])
+            self.ck_v[len(segs)].copy_(self.fwd.v[:n])
         self.checkpoints = [(self.ck_r[i], self.ck_v[i]) for i in range(len(segs))]
         self.final = (self.ck_r[len(segs)], self.ck_v[len(segs)])
         return self.fwd.r[:n, :3], self.fwd.v[:n, :3]
 
     def backward(self, g_r, g_v, stream=None):
-        """Gradients (dL/dr0 [n,3], dL/dv0 [n,3], dL/dGm [n]) from dL/dr_K, dL/dv_K."""
+        """Gradients (dL/dr0 [n,3], dL/dv0 [n,3], dL/dGm [n]) from dL/dr_K, dL/dv_K.
+        With graphs=True each segment (state reset, prepare and steps) replays from a
+        CUDA graph captured on first use."""
         a = self.adj
         n = a.info.n_bodies
-        a.gr.zero_()
-        a.gv.zero_()
-        a.ggm.zero_()
-        a.gr[:n, :3].copy_(g_r)
-        a.gv[:n, :3].copy_(g_v)
+        with torch.cuda.stream(self.fwd._stream(stream)):
+            a.gr.zero_()
+            a.gv.zero_()
+            a.ggm.zero_()
+            a.gr[:n, :3].copy_(g_r)
+            a.gv[:n, :3].copy_(g_v)
         segs = self._segments()
         for si in reversed(range(len(segs))):
             s0, s1 = segs[si]
-            # the exact stored state at the segment's end (the final state for the last)
-            a.set_state(self.ck_r[si + 1], self.ck_v[si + 1])
-            a.prepare(stream)
-            self._adj_steps(s1 - s0, stream)
+            if self.graphs:
+                self._graph(self._adj_graphs, si, a.device,
+                            lambda st, x=si, y=s0, z=s1: self._adj_segment(x, y, z, st)).replay()
+            else:
+                self._adj_segment(si, s0, s1, stream)
         self.reversed_state = (a.r[:n, :3].clone(), a.v[:n, :3].clone())
         return a.gr[:n, :3].clone(), a.gv[:n, :3].clone(), a.ggm[:n].clone()
 

@@ -17,29 +17,37 @@
 // reciprocal distance is selected to 0), so no large self terms enter the sums.
 //
 // The state needed by step k is not stored: the backward sweep reverses the forward
-// update in FP64,  r_k = r_{k+1} - T v_{k+1},  v_k = v_{k+1} - T a_k,  and recomputes
-// a_k = A(r_k) (stage 1) inside the same pair kernel as h and g.  The caller resets the
-// reversed state to the stored FP64 checkpoint at the start of every checkpoint
-// segment, so rounding in the reversal never accumulates over more than one segment.
+// update in FP64,  r_k = r_{k+1} - T v_{k+1},  v_k = v_{k+1} - T a_k.  a_k is either
+// the forward's own FP64 acceleration of that step, kept by the caller (grav_adjoint
+// a_in: what stage 2 wrote with GRAV_S2_WRITE_A), or recomputed as A(r_k) (stage 1)
+// inside the same pair kernel as h and g (a_in NULL).  The caller resets the reversed
+// state to the stored FP64 checkpoint at the start of every checkpoint segment, so
+// rounding in the reversal never accumulates over more than one segment.
 //
 // Pair kernel: persistent stage-1 work list (pairs_skeleton.cuh), j-tiles of FP32
 // positions (x, y, z, Gm) and FP32 u, FP32 tile partials folded into compensated
 // (TwoSum) FP32 sums, so no FP64 arithmetic runs in the pair loop; 7 outputs
-// per body (a, h, g) in the partial slots, as FP32 (hi, lo) pairs.  Adjoint stage 2 (1 or 8 lanes per padded row)
+// per body (a, h, g) in the partial slots, as FP32 (hi, lo) pairs, or 4 (h, g) when
+// the caller keeps the accelerations.  Adjoint stage 2 (1 or 8 lanes per padded row)
 // sums the slots and applies the updates above in FP64, then prepares the FP32
 // positions r_{k-1} and u for the next backward step.
+#include <algorithm>
+
 #include "pairs_skeleton.cuh"
 
 namespace grav {
 
 int record_error(int code, const char* msg);
 // the unique-pair backward pair kernel (adjoint_sym.cu)
-cudaError_t launch_vjp_sym(const grav_batch& b, const float4* upos, cudaStream_t st);
+cudaError_t launch_vjp_sym(const grav_batch& b, const float4* upos, bool fa, cudaStream_t st);
 int vjp_sym_occupancy(int bpt, int threads, int jtile, int* ctas_per_sm);
 
-template <int B_, int T_, int J_>
+// FA_: recompute the accelerations (slot components a, h, g) or not (h, g)
+template <int B_, int T_, int J_, bool FA_>
 struct VjpOp {
-	static constexpr int B = B_, T = T_, J = J_, NP = 2, NC = 7;
+	static constexpr bool FA = FA_;
+	static constexpr int B = B_, T = T_, J = J_, NP = 2, NC = FA ? 7 : 4;
+	static constexpr int H0 = FA ? 3 : 0, G0 = H0 + 3;
 	using Elem = float4;
 	const float4* pos;
 	const float4* upos;
@@ -90,9 +98,11 @@ struct VjpOp {
 				const float inv3 = inv2 * inv;
 				const float inv5 = inv3 * inv2;  // the -3 of Jf is applied at the fold
 				const float c = pj.w * inv3;  // Gm_j / r^3
-				fa[0][k] = fmaf(c, dx, fa[0][k]);
-				fa[1][k] = fmaf(c, dy, fa[1][k]);
-				fa[2][k] = fmaf(c, dz, fa[2][k]);
+				if constexpr (FA) {
+					fa[0][k] = fmaf(c, dx, fa[0][k]);
+					fa[1][k] = fmaf(c, dy, fa[1][k]);
+					fa[2][k] = fmaf(c, dz, fa[2][k]);
+				}
 				fs[k] += c;
 				fp[0][k] = fmaf(uj.x, inv3, fp[0][k]);
 				fp[1][k] = fmaf(uj.y, inv3, fp[1][k]);
@@ -112,7 +122,7 @@ struct VjpOp {
 		for (int k = 0; k < B; ++k) {
 #pragma unroll
 			for (int c3 = 0; c3 < 3; ++c3) {
-				two_sum_acc(ah[c3][k], al[c3][k], fa[c3][k]);
+				if constexpr (FA) two_sum_acc(ah[c3][k], al[c3][k], fa[c3][k]);
 				fa[c3][k] = 0.f;
 			}
 			const float ui[3] = {uxi[k], uyi[k], uzi[k]};
@@ -139,18 +149,18 @@ struct VjpOp {
 			const int i = tid + k * T;
 #pragma unroll
 			for (int c3 = 0; c3 < 3; ++c3) {
-				out2[c3 * IT + i] = make_float2(ah[c3][k], al[c3][k]);
-				out2[(3 + c3) * IT + i] = make_float2(hh[c3][k], hl[c3][k]);
+				if constexpr (FA) out2[c3 * IT + i] = make_float2(ah[c3][k], al[c3][k]);
+				out2[(H0 + c3) * IT + i] = make_float2(hh[c3][k], hl[c3][k]);
 			}
-			out2[6 * IT + i] = make_float2(gh[k], gl[k]);
+			out2[G0 * IT + i] = make_float2(gh[k], gl[k]);
 		}
 	}
 };
 
-template <int B, int T, int J>
+template <int B, int T, int J, bool FA>
 __global__ void __launch_bounds__(T) vjp_kernel(const grav_batch b, const float4* upos)
 {
-	VjpOp<B, T, J> op;
+	VjpOp<B, T, J, FA> op;
 	op.pos = static_cast<const float4*>(b.pos);
 	op.upos = upos;
 	run_pairs(b, op);
@@ -171,12 +181,16 @@ struct __align__(32) arow4 {
 constexpr int AS2_THREADS = 128;
 constexpr int ADJ_SPLIT_ROWS_MAX = 16384;  // ATPR = 8 up to this many padded rows, else 1
 
-template <int ATPR>
+// NC: components per slot entry, 7 (a, h, g) or 4 (h, g: the accelerations come from
+// a_in, the forward's own a_k rows).  With NC = 7 and a_in given, a_in is used.
+template <int ATPR, int NC>
 __global__ void __launch_bounds__(AS2_THREADS) adjoint_stage2_kernel(const grav_batch b,
-	double* gr, double* gv, double* ggm, float4* upos, const int flags)
+	double* gr, double* gv, double* ggm, float4* upos, const double* a_in, const int flags)
 {
 	static_assert(ATPR > 0 && ATPR <= 16 && (ATPR & (ATPR - 1)) == 0 && AS2_THREADS % 32 == 0,
 		"a row's lanes must sit in one warp");
+	static_assert(NC == 7 || NC == 4, "slot components");
+	constexpr int H0 = NC - 4, G0 = NC - 1;
 	const int64_t gthread = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
 	const int64_t g = gthread / ATPR;  // padded row; the ATPR lanes of a row share a warp
 	const int p = static_cast<int>(gthread % ATPR);
@@ -205,43 +219,52 @@ __global__ void __launch_bounds__(AS2_THREADS) adjoint_stage2_kernel(const grav_
 	arow4* grr = reinterpret_cast<arow4*>(gr);
 	arow4* gvv = reinterpret_cast<arow4*>(gv);
 	// lane 0 owns the row's update: its loads go out before the slot loads
-	arow4 r = {0.0, 0.0, 0.0, 0.0}, v = r, a_gr = r, a_gv = r;
+	arow4 r = {0.0, 0.0, 0.0, 0.0}, v = r, a_gr = r, a_gv = r, acc = r;
 	if (p == 0) {
 		r = rr[row];
 		v = vv[row];
 		a_gr = grr[row];
 		a_gv = gvv[row];
+		if ((flags & ADJ_STEP) && a_in) {  // read once: evict-first
+			const double2* ai = reinterpret_cast<const double2*>(a_in) + 2 * row;
+			const double2 axy = __ldcs(ai), az = __ldcs(ai + 1);
+			acc = arow4{axy.x, axy.y, az.x, 0.0};
+		}
 	}
 
-	double s[7] = {0, 0, 0, 0, 0, 0, 0};
+	double s[NC];
+#pragma unroll
+	for (int c = 0; c < NC; ++c) s[c] = 0.0;
 	if (flags & ADJ_STEP) {
 		// slots p, p + ATPR, ... hold FP32 (hi, lo) pairs; they are added in order into
 		// compensated FP32 sums (hi by TwoSum, lo and the errors into l), each round
 		// issuing all its loads first (the ones past the end are skipped), combined
 		// across the lanes by a TwoSum butterfly and widened once: no FP64 arithmetic
 		// per slot (GB300 runs FP64 at ~1/64 of the FP32 rate)
-		constexpr int SLOT_BATCH = 4;
-		const int64_t stride = 7 * static_cast<int64_t>(IT);  // 8-byte entries per slot
+		constexpr int SLOT_BATCH = NC == 4 ? 6 : 4;
+		const int64_t stride = NC * static_cast<int64_t>(IT);  // 8-byte entries per slot
 		// unique-pair plans: the last (row block index) slots of a segment are column
 		// slots holding FP32 values in their first half (adjoint_sym.cu)
 		const int nrow = b.mode == GRAV_MODE_FP32U ? S.nslots - S.il0 / IT : S.nslots;
 		const float2* part =
 			reinterpret_cast<const float2*>(b.part + static_cast<int64_t>(S.slot_base) * stride) + li;
-		float h[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, l[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+		float h[NC], l[NC];
+#pragma unroll
+		for (int c = 0; c < NC; ++c) h[c] = l[c] = 0.f;
 		for (int k = p; k < nrow; k += SLOT_BATCH * ATPR) {
 			const int m = min(SLOT_BATCH, (nrow - k + ATPR - 1) / ATPR);
-			float2 q[SLOT_BATCH][7];
+			float2 q[SLOT_BATCH][NC];
 #pragma unroll
 			for (int j = 0; j < SLOT_BATCH; ++j)
 				if (j < m) {
 #pragma unroll
-					for (int c = 0; c < 7; ++c) q[j][c] = __ldg(part + (k + j * ATPR) * stride + c * IT);
+					for (int c = 0; c < NC; ++c) q[j][c] = __ldg(part + (k + j * ATPR) * stride + c * IT);
 				}
 #pragma unroll
 			for (int j = 0; j < SLOT_BATCH; ++j)
 				if (j < m) {
 #pragma unroll
-					for (int c = 0; c < 7; ++c) {
+					for (int c = 0; c < NC; ++c) {
 						two_sum_acc(h[c], l[c], q[j][c].x);
 						l[c] += q[j][c].y;
 					}
@@ -250,20 +273,20 @@ __global__ void __launch_bounds__(AS2_THREADS) adjoint_stage2_kernel(const grav_
 		const float* cpart =
 			reinterpret_cast<const float*>(b.part + static_cast<int64_t>(S.slot_base) * stride) + li;
 		for (int k = nrow + p; k < S.nslots; k += SLOT_BATCH * ATPR) {
-			float q[SLOT_BATCH][7];
+			float q[SLOT_BATCH][NC];
 #pragma unroll
 			for (int j = 0; j < SLOT_BATCH; ++j)
 #pragma unroll
-				for (int c = 0; c < 7; ++c)  // loads past the end read as 0, added exactly
+				for (int c = 0; c < NC; ++c)  // loads past the end read as 0, added exactly
 					q[j][c] = (k + j * ATPR < S.nslots) ? __ldg(cpart + (k + j * ATPR) * 2 * stride + c * IT)
 					                                  : 0.f;
 #pragma unroll
 			for (int j = 0; j < SLOT_BATCH; ++j)
 #pragma unroll
-				for (int c = 0; c < 7; ++c) two_sum_acc(h[c], l[c], q[j][c]);
+				for (int c = 0; c < NC; ++c) two_sum_acc(h[c], l[c], q[j][c]);
 		}
 #pragma unroll
-		for (int c = 0; c < 7; ++c) {
+		for (int c = 0; c < NC; ++c) {
 			group_sum_pair<ATPR>(h[c], l[c], gmask);
 			s[c] = static_cast<double>(h[c]) + static_cast<double>(l[c]);
 		}
@@ -272,21 +295,22 @@ __global__ void __launch_bounds__(AS2_THREADS) adjoint_stage2_kernel(const grav_
 
 	if (flags & ADJ_STEP) {
 		// reverse the forward update: r_k = r_{k+1} - T v_{k+1}; v_k = v_{k+1} - T a_k
+		if (NC == 7 && !a_in) acc = arow4{s[0], s[1], s[2], 0.0};
 		r.x = __dsub_rn(r.x, __dmul_rn(v.x, T));
 		r.y = __dsub_rn(r.y, __dmul_rn(v.y, T));
 		r.z = __dsub_rn(r.z, __dmul_rn(v.z, T));
-		v.x = __dsub_rn(v.x, __dmul_rn(s[0], T));
-		v.y = __dsub_rn(v.y, __dmul_rn(s[1], T));
-		v.z = __dsub_rn(v.z, __dmul_rn(s[2], T));
+		v.x = __dsub_rn(v.x, __dmul_rn(acc.x, T));
+		v.y = __dsub_rn(v.y, __dmul_rn(acc.y, T));
+		v.z = __dsub_rn(v.z, __dmul_rn(acc.z, T));
 		// gradients
 		const double ux = a_gv.x + T * a_gr.x, uy = a_gv.y + T * a_gr.y, uz = a_gv.z + T * a_gr.z;
-		a_gr.x += T * s[3];
-		a_gr.y += T * s[4];
-		a_gr.z += T * s[5];
+		a_gr.x += T * s[H0];
+		a_gr.y += T * s[H0 + 1];
+		a_gr.z += T * s[H0 + 2];
 		a_gv.x = ux;
 		a_gv.y = uy;
 		a_gv.z = uz;
-		ggm[row] -= T * s[6];
+		ggm[row] -= T * s[G0];
 		rr[row] = r;
 		vv[row] = v;
 		grr[row] = a_gr;
@@ -305,8 +329,8 @@ __global__ void __launch_bounds__(AS2_THREADS) adjoint_stage2_kernel(const grav_
 }
 
 // Adjoint stage 2 as a programmatic dependent of the kernel before it (it waits with
-// grid_dep_wait); 8 lanes per padded row for small batches, else 1.
-cudaError_t launch_adjoint_stage2(const grav_batch& b, const grav_adjoint& a, int flags,
+// grid_dep_wait); 8 lanes per padded row for small batches, else 1; nc slot components.
+cudaError_t launch_adjoint_stage2(const grav_batch& b, const grav_adjoint& a, int flags, int nc,
 	cudaStream_t st)
 {
 	grav_batch copy = b;
@@ -314,31 +338,40 @@ cudaError_t launch_adjoint_stage2(const grav_batch& b, const grav_adjoint& a, in
 	double* gv = static_cast<double*>(a.gv);
 	double* ggm = static_cast<double*>(a.ggm);
 	float4* upos = static_cast<float4*>(a.upos);
+	const double* a_in = a.a_in;
 	int f = flags;
-	void* args[] = {&copy, &gr, &gv, &ggm, &upos, &f};
+	void* args[] = {&copy, &gr, &gv, &ggm, &upos, &a_in, &f};
 	const int atpr = b.n_pad_total <= ADJ_SPLIT_ROWS_MAX ? 8 : 1;
 	const unsigned blocks =
 		static_cast<unsigned>((b.n_pad_total * atpr + AS2_THREADS - 1) / AS2_THREADS);
-	const void* fn = atpr == 8 ? reinterpret_cast<const void*>(&adjoint_stage2_kernel<8>)
-	                           : reinterpret_cast<const void*>(&adjoint_stage2_kernel<1>);
+	const void* fn = nc == 4
+		? (atpr == 8 ? reinterpret_cast<const void*>(&adjoint_stage2_kernel<8, 4>)
+		             : reinterpret_cast<const void*>(&adjoint_stage2_kernel<1, 4>))
+		: (atpr == 8 ? reinterpret_cast<const void*>(&adjoint_stage2_kernel<8, 7>)
+		             : reinterpret_cast<const void*>(&adjoint_stage2_kernel<1, 7>));
 	return launch_dependent(fn, blocks, AS2_THREADS, 0, st, args);
 }
 
 struct VjpKernel {
 	int bpt, threads, jtile;
+	bool fa;
 	const void* fn;
 	int smem;
 };
 
-#define GRAV_VJP_ENTRY(B, T, J) \
-	{B, T, J, reinterpret_cast<const void*>(&vjp_kernel<B, T, J>), \
-		pairs_smem_bytes<VjpOp<B, T, J>>()}
+#define GRAV_VJP_ENTRY(B, T, J, FA) \
+	{B, T, J, FA, reinterpret_cast<const void*>(&vjp_kernel<B, T, J, FA>), \
+		pairs_smem_bytes<VjpOp<B, T, J, FA>>()}
 
 static const VjpKernel k_vjp[] = {
-	GRAV_VJP_ENTRY(1, 128, 128),
-	GRAV_VJP_ENTRY(2, 128, 128),
-	GRAV_VJP_ENTRY(2, 256, 128),
-	GRAV_VJP_ENTRY(4, 128, 128),
+	GRAV_VJP_ENTRY(1, 128, 128, true),
+	GRAV_VJP_ENTRY(2, 128, 128, true),
+	GRAV_VJP_ENTRY(2, 256, 128, true),
+	GRAV_VJP_ENTRY(4, 128, 128, true),
+	GRAV_VJP_ENTRY(1, 128, 128, false),
+	GRAV_VJP_ENTRY(2, 128, 128, false),
+	GRAV_VJP_ENTRY(2, 256, 128, false),
+	GRAV_VJP_ENTRY(4, 128, 128, false),
 };
 
 int vjp_table(const VjpKernel** out)
@@ -400,16 +433,18 @@ extern "C" int grav_adjoint_occupancy(int mode, const grav_tile* t, int32_t* cta
 	if (mode != GRAV_MODE_FP32) return grav::record_error(GRAV_E_ARG, "adjoint mode must be FP32 or FP32U");
 	const grav::VjpKernel* tab = nullptr;
 	const int n = grav::vjp_table(&tab);
+	int best = -1;  // the smaller of the two variants' (the plan's grid serves both)
 	for (int i = 0; i < n; ++i)
 		if (tab[i].bpt == t->bpt && tab[i].threads == t->threads && tab[i].jtile == t->jtile) {
 			int blocks = 0;
 			cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, tab[i].fn,
 				tab[i].threads, tab[i].smem);
 			if (e != cudaSuccess) return grav::record_error(GRAV_E_CUDA, cudaGetErrorString(e));
-			*ctas_per_sm = blocks;
-			return GRAV_OK;
+			best = best < 0 ? blocks : std::min(best, blocks);
 		}
-	return grav::record_error(GRAV_E_TILE, "tile shape has no adjoint kernel");
+	if (best < 0) return grav::record_error(GRAV_E_TILE, "tile shape has no adjoint kernel");
+	*ctas_per_sm = best;
+	return GRAV_OK;
 }
 
 extern "C" int grav_adjoint_prepare(const grav_adjoint* a, void* stream)
@@ -420,7 +455,7 @@ extern "C" int grav_adjoint_prepare(const grav_adjoint* a, void* stream)
 	if (b.n_pad_total == 0) return GRAV_OK;
 	grav_batch copy = b;
 	copy.part = a->part7;
-	cudaError_t e = grav::launch_adjoint_stage2(copy, *a, ADJ_PREPARE, static_cast<cudaStream_t>(stream));
+	cudaError_t e = grav::launch_adjoint_stage2(copy, *a, ADJ_PREPARE, 7, static_cast<cudaStream_t>(stream));
 	return e == cudaSuccess ? GRAV_OK : grav::record_error(GRAV_E_CUDA, cudaGetErrorString(e));
 }
 
@@ -433,12 +468,14 @@ extern "C" int grav_adjoint_step(const grav_adjoint* a, void* stream)
 	cudaStream_t st = static_cast<cudaStream_t>(stream);
 	grav_batch copy = b;
 	copy.part = a->part7;
+	// with the forward's accelerations at hand the pair kernel forms only h and g
+	const bool fa = a->a_in == nullptr;
 	if (b.n_units > 0) {
 		if (b.tile.grid <= 0 || b.tile.grid > b.n_units)
 			return grav::record_error(GRAV_E_ARG, "tile.grid must be in [1, n_units]");
 		const float4* up = static_cast<const float4*>(a->upos);
 		if (b.mode == GRAV_MODE_FP32U) {
-			const cudaError_t e = grav::launch_vjp_sym(copy, up, st);
+			const cudaError_t e = grav::launch_vjp_sym(copy, up, fa, st);
 			if (e == cudaErrorInvalidValue)
 				return grav::record_error(GRAV_E_TILE, "tile shape has no unique-pair adjoint kernel");
 			if (e != cudaSuccess) return grav::record_error(GRAV_E_CUDA, cudaGetErrorString(e));
@@ -448,7 +485,7 @@ extern "C" int grav_adjoint_step(const grav_adjoint* a, void* stream)
 			const grav::VjpKernel* k = nullptr;
 			for (int i = 0; i < n; ++i)
 				if (tab[i].bpt == b.tile.bpt && tab[i].threads == b.tile.threads &&
-					tab[i].jtile == b.tile.jtile)
+					tab[i].jtile == b.tile.jtile && tab[i].fa == fa)
 					k = &tab[i];
 			if (!k) return grav::record_error(GRAV_E_TILE, "tile shape has no adjoint kernel");
 			void* args[] = {&copy, &up};
@@ -456,6 +493,6 @@ extern "C" int grav_adjoint_step(const grav_adjoint* a, void* stream)
 			if (e != cudaSuccess) return grav::record_error(GRAV_E_CUDA, cudaGetErrorString(e));
 		}
 	}
-	cudaError_t e = grav::launch_adjoint_stage2(copy, *a, ADJ_STEP | ADJ_PREPARE, st);
+	cudaError_t e = grav::launch_adjoint_stage2(copy, *a, ADJ_STEP | ADJ_PREPARE, fa ? 7 : 4, st);
 	return e == cudaSuccess ? GRAV_OK : grav::record_error(GRAV_E_CUDA, cudaGetErrorString(e));
 }

@@ -1,31 +1,35 @@
 // adjoint_sym.cu -- the backward pair kernel over unique pairs.
 //
 // Same transposed step as adjoint.cu (derivation there), with each unordered pair (i, j)
-// visited once.  For d = r_j - r_i, inv3 = |d|^-3, inv5 = |d|^-5 (0 at zero separation)
-// and dw = Gm_i (d.u_j) - Gm_j (d.u_i):
-//   row i    a_i += Gm_j inv3 d            h_i: P += inv3 u_j, S += Gm_j inv3, Q += inv5 dw d
+// visited once.  For d = r_j - r_i, inv3 = |d|^-3, inv2 = |d|^-2 (both 0 at zero
+// separation), ci = Gm_j inv3, cj = Gm_i inv3 and t5 = (cj (d.u_j) - ci (d.u_i)) inv2
+// (= (Gm_i d.u_j - Gm_j d.u_i) / |d|^5):
+//   row i    a_i += ci d                   h_i: P += inv3 u_j, S += ci, Q += t5 d
 //            g_i += inv3 (d.u_j)           (h_i = Gm_i P - u_i S - 3 Q, formed per tile)
-//   column j a_j -= Gm_i inv3 d            h_j += Gm_j inv3 u_i - Gm_i inv3 u_j + 3 inv5 dw d
+//   column j a_j -= cj d                   h_j += ci u_i - cj u_j + 3 t5 d
 //            g_j -= inv3 (d.u_i)
 // since Jf(-d) = Jf(d) (Jf(d) = I/|d|^3 - 3 d d^T/|d|^5) and the pair's h terms for j are
-// those for i with the roles of the bodies swapped.  47 FMA-pipe operations and one
-// MUFU per unordered pair, against 2 x 33 when both ordered pairs are visited.
+// those for i with the roles of the bodies swapped.  With the accelerations (FA = true:
+// the forward's a_k is recomputed here) that is 46 FMA-pipe operations and one MUFU per
+// unordered pair, against 2 x 33 when both ordered pairs are visited; when the caller
+// keeps the forward's accelerations (FA = false) the a terms drop out: 40 operations and
+// 4 rotating column values instead of 7.
 //
 // Decomposition: the plan of grav_plan_pairs and the warp scheme of stage1_sym.cu.  Row
 // block I's units are the j-tiles of blocks J >= I; a j-tile of block I itself is done
 // with every ordered pair, rows only; a j-tile of a block J > I on unique pairs: lane l
-// meets body (l + s) mod 32 of a 32-body chunk at step s while the chunk's 7 column
+// meets body (l + s) mod 32 of a 32-body chunk at step s while the chunk's column
 // values rotate one lane per step, then warps add them into shared memory and the tile's
 // column sums go, as FP32, to the column slot of (I, J) (block J's last J slots).  Row
 // sums are compensated FP32 (TwoSum) and go out as FP32 (hi, lo) pairs.  Slot layout
-// [slot][7][R]: a, h, g.
+// [slot][NC][R]: a, h, g (NC = 7) or h, g (NC = 4).
 #include "grav_device.cuh"
 
 namespace grav {
 
 int record_error(int code, const char* msg);
 
-template <int B, int W, int JT>
+template <int B, int W, int JT, bool FA>
 __global__ void __launch_bounds__(32 * W) vjp_sym_kernel(const grav_batch b,
 	const float4* __restrict__ upos)
 {
@@ -33,7 +37,9 @@ __global__ void __launch_bounds__(32 * W) vjp_sym_kernel(const grav_batch b,
 	constexpr int R = T * B;      // rows per block (= itile)
 	constexpr int TPB = R / JT;   // j-tiles per block
 	constexpr int NCH = JT / 32;  // 32-body chunks per j-tile
-	constexpr int NC = 7;         // a (3), h (3), g
+	constexpr int NC = FA ? 7 : 4;  // [a (3),] h (3), g
+	constexpr int H0 = FA ? 3 : 0;  // first h component of a slot
+	constexpr int G0 = H0 + 3;      // the g component
 	constexpr uint32_t TILE_BYTES = JT * sizeof(float4);
 	static_assert(R % JT == 0 && JT % 32 == 0 && (NCH & (NCH - 1)) == 0, "tile shapes");
 	extern __shared__ __align__(128) float4 vs_tiles[];  // [2 buffers][pos, u][JT]
@@ -145,9 +151,11 @@ __global__ void __launch_bounds__(32 * W) vjp_sym_kernel(const grav_batch b,
 						const float inv3 = inv2 * inv;
 						const float inv5 = inv3 * inv2;
 						const float ci = pj.w * inv3;
-						fa[0][k] = fmaf(ci, dx, fa[0][k]);
-						fa[1][k] = fmaf(ci, dy, fa[1][k]);
-						fa[2][k] = fmaf(ci, dz, fa[2][k]);
+						if constexpr (FA) {
+							fa[0][k] = fmaf(ci, dx, fa[0][k]);
+							fa[1][k] = fmaf(ci, dy, fa[1][k]);
+							fa[2][k] = fmaf(ci, dz, fa[2][k]);
+						}
 						fs[k] += ci;
 						fp[0][k] = fmaf(uj.x, inv3, fp[0][k]);
 						fp[1][k] = fmaf(uj.y, inv3, fp[1][k]);
@@ -180,28 +188,31 @@ __global__ void __launch_bounds__(32 * W) vjp_sym_kernel(const grav_batch b,
 							const float inv = (r2 > 0.f) ? rsqrt_sfu(r2) : 0.f;
 							const float inv2 = inv * inv;
 							const float inv3 = inv2 * inv;
-							const float inv5 = inv3 * inv2;
 							const float ci = pj.w * inv3;   // Gm_j / r^3
 							const float cj = gi[k] * inv3;  // Gm_i / r^3
 							// row i
-							fa[0][k] = fmaf(ci, dx, fa[0][k]);
-							fa[1][k] = fmaf(ci, dy, fa[1][k]);
-							fa[2][k] = fmaf(ci, dz, fa[2][k]);
+							if constexpr (FA) {
+								fa[0][k] = fmaf(ci, dx, fa[0][k]);
+								fa[1][k] = fmaf(ci, dy, fa[1][k]);
+								fa[2][k] = fmaf(ci, dz, fa[2][k]);
+							}
 							fs[k] += ci;
 							fp[0][k] = fmaf(uj.x, inv3, fp[0][k]);
 							fp[1][k] = fmaf(uj.y, inv3, fp[1][k]);
 							fp[2][k] = fmaf(uj.z, inv3, fp[2][k]);
 							const float duj = fmaf(dz, uj.z, fmaf(dy, uj.y, dx * uj.x));
 							const float dui = fmaf(dz, uzi[k], fmaf(dy, uyi[k], dx * uxi[k]));
-							const float t5 = fmaf(gi[k], duj, -pj.w * dui) * inv5;
+							const float t5 = fmaf(cj, duj, -ci * dui) * inv2;
 							fq[0][k] = fmaf(t5, dx, fq[0][k]);
 							fq[1][k] = fmaf(t5, dy, fq[1][k]);
 							fq[2][k] = fmaf(t5, dz, fq[2][k]);
 							fg[k] = fmaf(duj, inv3, fg[k]);
 							// column j
-							cax = fmaf(-cj, dx, cax);
-							cay = fmaf(-cj, dy, cay);
-							caz = fmaf(-cj, dz, caz);
+							if constexpr (FA) {
+								cax = fmaf(-cj, dx, cax);
+								cay = fmaf(-cj, dy, cay);
+								caz = fmaf(-cj, dz, caz);
+							}
 							const float t3 = 3.f * t5;
 							chx = fmaf(t3, dx, fmaf(-cj, uj.x, fmaf(ci, uxi[k], chx)));
 							chy = fmaf(t3, dy, fmaf(-cj, uj.y, fmaf(ci, uyi[k], chy)));
@@ -209,22 +220,26 @@ __global__ void __launch_bounds__(32 * W) vjp_sym_kernel(const grav_batch b,
 							cg = fmaf(-dui, inv3, cg);
 						}
 						const int src = (lane + 1) & 31;
-						cax = __shfl_sync(0xffffffffu, cax, src);
-						cay = __shfl_sync(0xffffffffu, cay, src);
-						caz = __shfl_sync(0xffffffffu, caz, src);
+						if constexpr (FA) {
+							cax = __shfl_sync(0xffffffffu, cax, src);
+							cay = __shfl_sync(0xffffffffu, cay, src);
+							caz = __shfl_sync(0xffffffffu, caz, src);
+						}
 						chx = __shfl_sync(0xffffffffu, chx, src);
 						chy = __shfl_sync(0xffffffffu, chy, src);
 						chz = __shfl_sync(0xffffffffu, chz, src);
 						cg = __shfl_sync(0xffffffffu, cg, src);
 					}
 					const int ci0 = ch * 32 + lane;
-					atomicAdd(&colacc[0][ci0], cax);
-					atomicAdd(&colacc[1][ci0], cay);
-					atomicAdd(&colacc[2][ci0], caz);
-					atomicAdd(&colacc[3][ci0], chx);
-					atomicAdd(&colacc[4][ci0], chy);
-					atomicAdd(&colacc[5][ci0], chz);
-					atomicAdd(&colacc[6][ci0], cg);
+					if constexpr (FA) {
+						atomicAdd(&colacc[0][ci0], cax);
+						atomicAdd(&colacc[1][ci0], cay);
+						atomicAdd(&colacc[2][ci0], caz);
+					}
+					atomicAdd(&colacc[H0][ci0], chx);
+					atomicAdd(&colacc[H0 + 1][ci0], chy);
+					atomicAdd(&colacc[H0 + 2][ci0], chz);
+					atomicAdd(&colacc[G0][ci0], cg);
 				}
 				__syncthreads();
 				// column sums of this tile -> column slot of (I, J) as FP32, then clear
@@ -247,7 +262,7 @@ __global__ void __launch_bounds__(32 * W) vjp_sym_kernel(const grav_batch b,
 				const float ui[3] = {uxi[k], uyi[k], uzi[k]};
 #pragma unroll
 				for (int q3 = 0; q3 < 3; ++q3) {
-					two_sum_acc(ah[q3][k], al[q3][k], fa[q3][k]);
+					if constexpr (FA) two_sum_acc(ah[q3][k], al[q3][k], fa[q3][k]);
 					// h = Gm_i P - u_i S - 3 Q
 					const float ht = fmaf(gi[k], fp[q3][k], fmaf(-ui[q3], fs[k], -3.f * fq[q3][k]));
 					two_sum_acc(hh[q3][k], hl[q3][k], ht);
@@ -268,10 +283,10 @@ __global__ void __launch_bounds__(32 * W) vjp_sym_kernel(const grav_batch b,
 			const int i = r0 + k * 32;
 #pragma unroll
 			for (int q3 = 0; q3 < 3; ++q3) {
-				out[q3 * R + i] = make_float2(ah[q3][k], al[q3][k]);
-				out[(3 + q3) * R + i] = make_float2(hh[q3][k], hl[q3][k]);
+				if constexpr (FA) out[q3 * R + i] = make_float2(ah[q3][k], al[q3][k]);
+				out[(H0 + q3) * R + i] = make_float2(hh[q3][k], hl[q3][k]);
 			}
-			out[6 * R + i] = make_float2(gh[k], gl[k]);
+			out[G0 * R + i] = make_float2(gh[k], gl[k]);
 		}
 		ub = S.unit_begin + t1;
 		++s;
@@ -289,47 +304,56 @@ __global__ void __launch_bounds__(32 * W) vjp_sym_kernel(const grav_batch b,
 
 struct VjpSymKernel {
 	int bpt, threads, jtile;
+	bool fa;
 	const void* fn;
 	int smem;
 };
 
-#define GRAV_VJPSYM_ENTRY(B, W, J) \
-	{B, 32 * W, J, reinterpret_cast<const void*>(&vjp_sym_kernel<B, W, J>), 2 * 2 * J * 16}
+#define GRAV_VJPSYM_ENTRY(B, W, J, FA) \
+	{B, 32 * W, J, FA, reinterpret_cast<const void*>(&vjp_sym_kernel<B, W, J, FA>), 2 * 2 * J * 16}
 
 static const VjpSymKernel k_vjp_sym[] = {
-	GRAV_VJPSYM_ENTRY(2, 8, 64),
-	GRAV_VJPSYM_ENTRY(2, 4, 64),
-	GRAV_VJPSYM_ENTRY(4, 4, 128),
+	GRAV_VJPSYM_ENTRY(2, 8, 64, true),
+	GRAV_VJPSYM_ENTRY(2, 4, 64, true),
+	GRAV_VJPSYM_ENTRY(4, 4, 128, true),
+	GRAV_VJPSYM_ENTRY(2, 8, 64, false),
+	GRAV_VJPSYM_ENTRY(2, 4, 64, false),
+	GRAV_VJPSYM_ENTRY(4, 4, 128, false),
 };
 
-const VjpSymKernel* find_vjp_sym(int bpt, int threads, int jtile)
+const VjpSymKernel* find_vjp_sym(int bpt, int threads, int jtile, bool fa)
 {
 	for (const VjpSymKernel& k : k_vjp_sym)
-		if (k.bpt == bpt && k.threads == threads && k.jtile == jtile) return &k;
+		if (k.bpt == bpt && k.threads == threads && k.jtile == jtile && k.fa == fa) return &k;
 	return nullptr;
 }
 
 // Launch the unique-pair backward pair kernel (programmatic dependent; it waits with
-// grid_dep_wait before it reads).  Returns cudaErrorInvalidValue for a shape that is not
-// compiled.
-cudaError_t launch_vjp_sym(const grav_batch& b, const float4* upos, cudaStream_t st)
+// grid_dep_wait before it reads); fa: recompute the accelerations (7 slot components)
+// or not (4).  Returns cudaErrorInvalidValue for a shape that is not compiled.
+cudaError_t launch_vjp_sym(const grav_batch& b, const float4* upos, bool fa, cudaStream_t st)
 {
-	const VjpSymKernel* k = find_vjp_sym(b.tile.bpt, b.tile.threads, b.tile.jtile);
+	const VjpSymKernel* k = find_vjp_sym(b.tile.bpt, b.tile.threads, b.tile.jtile, fa);
 	if (!k) return cudaErrorInvalidValue;
 	grav_batch copy = b;
 	void* args[] = {&copy, &upos};
 	return launch_dependent(k->fn, b.tile.grid, k->threads, k->smem, st, args);
 }
 
+// Resident CTAs per SM: the smaller of the two variants' (the plan's grid serves both).
 int vjp_sym_occupancy(int bpt, int threads, int jtile, int* ctas_per_sm)
 {
-	const VjpSymKernel* k = find_vjp_sym(bpt, threads, jtile);
-	if (!k) return 0;
-	int occ = 0;
-	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k->fn, k->threads, k->smem) !=
-		cudaSuccess)
-		return -1;
-	*ctas_per_sm = occ;
+	int best = -1;
+	for (const bool fa : {true, false}) {
+		const VjpSymKernel* k = find_vjp_sym(bpt, threads, jtile, fa);
+		if (!k) return 0;
+		int occ = 0;
+		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k->fn, k->threads, k->smem) !=
+			cudaSuccess)
+			return -1;
+		best = best < 0 ? occ : min(best, occ);
+	}
+	*ctas_per_sm = best;
 	return 1;
 }
 

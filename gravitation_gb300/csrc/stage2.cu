@@ -180,8 +180,14 @@ __global__ void __launch_bounds__(S2_THREADS) stage2_kernel(const grav_batch b, 
 	if (p != 0) return;
 
 	if (!(flags & GRAV_S2_PREPARE)) {
-		if ((flags & GRAV_S2_WRITE_A) && b.a_out)
-			reinterpret_cast<drow4*>(b.a_out)[row] = drow4{ax, ay, az, 0.0};
+		if ((flags & GRAV_S2_WRITE_A) && b.a_out) {
+			// streaming stores: a caller that keeps every step's accelerations writes a
+			// new buffer each step, which must not push the step's own working set
+			// (positions, slots, state) out of L2
+			double2* ao = reinterpret_cast<double2*>(b.a_out) + 2 * row;
+			__stcs(ao, make_double2(ax, ay));
+			__stcs(ao + 1, make_double2(az, 0.0));
+		}
 		if (integrate) {
 			const double T = U.T;
 			v.x = __dadd_rn(__dmul_rn(ax, T), v.x);

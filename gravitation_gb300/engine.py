@@ -93,6 +93,53 @@ def make_plan(sizes, T, tile, mode='fp32'):
     return info, univ, seg
 
 
+def plan_part_bytes(sizes, tile, mode, comps=3):
+    """Bytes of partial-sum slots the plan of `mode` (all pairs or unique pairs) needs for
+    `sizes` with `tile`: grav_part_bytes, scaled to `comps` components per slot entry (3
+    for stage 1; the backward pair kernel keeps 7).  Host-side, no GPU needed.
+
+    The unique-pair plan keeps one column slot per pair of row blocks, so its slots grow
+    as N^2 / (rows per block): 12.9 GB at N = 2^20 with 1024-row blocks, 206 GB at 2^22.
+    The all-pairs plan keeps one slot per CTA piece of a row block: 36 MB at 2^20."""
+    L = _lib.load()
+    fn = L.grav_plan_pairs if mode in _lib.PAIR_MODES else L.grav_plan
+    sizes = [int(x) for x in sizes]
+    nu = len(sizes)
+    n_arr = (ctypes.c_int32 * max(nu, 1))(*sizes)
+    T_arr = (ctypes.c_double * max(nu, 1))(*([1.0] * max(nu, 1)))
+    t = _lib.Tile(tile.bpt, tile.threads, tile.jtile, max(int(tile.grid), 1))
+    info = _lib.PlanInfo()
+    check(fn(nu, n_arr, T_arr, ctypes.byref(t), ctypes.byref(info), None, None))
+    return int(L.grav_part_bytes(ctypes.byref(info))) * comps // 3
+
+
+SLOT_BUDGET_FRACTION = 0.125
+SLOT_BUDGET_NO_GPU = 32 << 30
+
+
+def slot_budget_bytes(device=None):
+    """Device memory that a unique-pair plan chosen by default may spend on partial-sum
+    slots: an eighth of the GPU's memory (about 35 GB on a GB300); 32 GiB when no GPU is
+    visible (host-side planning)."""
+    if not torch.cuda.is_available():
+        return SLOT_BUDGET_NO_GPU
+    idx = torch.cuda.current_device() if device is None else torch.device(device).index
+    if idx is None:
+        idx = torch.cuda.current_device()
+    return int(torch.cuda.get_device_properties(idx).total_memory * SLOT_BUDGET_FRACTION)
+
+
+def pair_plan_fits(sizes, budget=None, mode='fp32u', comps=3, tiles=None):
+    """True when the unique-pair plan's slots stay within `budget` bytes (default
+    slot_budget_bytes()) for every shape in `tiles` (default: every compiled shape of
+    `mode`, so that whatever the autotuner picks fits)."""
+    if budget is None:
+        budget = slot_budget_bytes()
+    if tiles is None:
+        tiles = tile_list(mode)
+    return all(plan_part_bytes(sizes, t, mode, comps) <= budget for t in tiles)
+
+
 def _ctypes_to_device(arr, nbytes, device):
     host = torch.frombuffer(bytearray(ctypes.string_at(ctypes.addressof(arr), nbytes)),
                             dtype=torch.uint8) if nbytes else torch.zeros(0, dtype=torch.uint8)
@@ -116,6 +163,10 @@ def default_tile(mode, sizes, device=None):
         t.grid = grid
         pinfo, _, _ = make_plan(sizes, 1.0, t, mode)
         if pinfo.n_units == 0:
+            # no pairs at all (only empty universes): stage 1 launches nothing, any
+            # compiled shape serves
+            if best is None:
+                best = (float('inf'), _lib.Tile(t.bpt, t.threads, t.jtile, grid))
             continue
         # padded work (interactions) and the slowest CTA's share of it
         work = pinfo.n_units * pinfo.itile * t.jtile

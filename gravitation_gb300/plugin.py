@@ -56,10 +56,16 @@ _DTYPE_MODE = {'float32': 'fp32', 'float64': 'fp64'}
 UNIQUE_PAIRS_FROM_N = 8192
 
 
-def default_mode(dtype, n):
+def default_mode(dtype, n, budget=None):
+    """Precision mode for a dtype and body count: float32 runs on unique pairs from
+    UNIQUE_PAIRS_FROM_N bodies while the unique-pair plan's partial-sum slots fit the
+    slot budget (engine.slot_budget_bytes, or `budget` bytes), on all pairs otherwise
+    (above ~1.7 million bodies on a GB300)."""
     mode = _DTYPE_MODE.get(str(dtype))
     if mode == 'fp32' and n >= UNIQUE_PAIRS_FROM_N:
-        mode = 'fp32u'
+        from .engine import pair_plan_fits
+        if pair_plan_fits([n], budget):
+            mode = 'fp32u'
     return mode
 
 

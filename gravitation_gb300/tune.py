@@ -111,6 +111,8 @@ class Tuner:
         t = self.lookup(mode, sizes, dev_info)
         if t is not None:
             return t
+        if sum(int(n) for n in sizes) == 0:
+            return default_tile(mode, sizes, dev_info.index)   # nothing to time
         if tune_if_missing is None:
             tune_if_missing = os.environ.get('GRAV_AUTOTUNE', '1') != '0'
         if tune_if_missing:
@@ -122,7 +124,8 @@ class Tuner:
         `grid_factors` x (SMs x resident CTAs), on a seeded state and cache the fastest.
         What is timed is the full step (stage 1 + stage 2) replayed from a CUDA graph: a
         smaller grid gives each CTA more work units but leaves fewer partial-sum slots
-        per row for stage 2, which at a few thousand bodies is worth as much."""
+        per row for stage 2, which at a few thousand bodies is worth as much.  Above
+        2^38 interactions per step a replay holds one step instead of `reps`."""
         import torch
         from .engine import Engine, occupancy, tile_list
         from .scenarios import uniform_cube
@@ -138,6 +141,10 @@ class Tuner:
         gm = np.concatenate(ms) if ms else np.zeros(0)
         best = None
         seen = set()
+        if sum(n * n for n in sizes) >= 1 << 38:
+            # steps of 0.1 s and more (above ~500k bodies): one step per replay is
+            # already far above the timing noise, and keeps tuning to about a minute
+            reps = 1
         for cand in tile_list(mode):
             occ = occupancy(mode, cand, dev_info.index)
             if occ <= 0:

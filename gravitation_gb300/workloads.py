@@ -62,7 +62,10 @@ def run_adjoint(n=4096, steps=1000, every=32, seed=3, reps=3, tuner=None, device
                 'ratio_fwd_plus_adjoint_over_fwd': t / f,
                 'fwd_adjoint_steps_per_s': steps / (t * 1e-3),
                 'forward_tile': [ro.fwd.tile.bpt, ro.fwd.tile.threads, ro.fwd.tile.jtile,
-                                 ro.fwd.info.grid]}
+                                 ro.fwd.info.grid],
+                'backward_kernel': '%s, %s' % (
+                    'unique pairs' if ro.adj.pairs else 'all pairs',
+                    'forward accelerations kept' if ro.store_a else 'accelerations recomputed')}
 
     out = {'workload': 'N=%d uniform cube seed %d, %d steps, checkpoint every %d, loss = mean '
                        '|r_K - r_target|^2 (target: masses x U[0.99,1.01])' % (n, seed, steps,

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define GRAV_ABI_VERSION 2
+#define GRAV_ABI_VERSION 3
 
 /* status codes */
 #define GRAV_OK 0
@@ -236,6 +236,9 @@ typedef struct grav_adjoint {
 	double* ggm;   /* n_bodies: dL/d(G m), accumulated (in/out) */
 	void* upos;    /* float4 [n_pad_total]: scratch, FP32 u = gv + T gr of the next step */
 	double* part7; /* n_slots x 7 x itile doubles: scratch */
+	const double* a_in; /* n_bodies x 4: the forward's accelerations a_k of the step being
+	                       reversed (as stage 2 wrote them with GRAV_S2_WRITE_A), or NULL:
+	                       the pair kernel then recomputes them */
 } grav_adjoint;
 
 /* 1 if `tile` has a compiled adjoint pair kernel for `mode` (GRAV_MODE_FP32: all
@@ -252,9 +255,9 @@ int grav_adjoint_prepare(const grav_adjoint* a, void* stream);
 
 /*
  * One backward step through stage 2 and stage 1 (the adjoint kernel pair): a pair
- * kernel recomputes a_k = A(r_k) (stage 1) and forms h = J_A(r_k)^T u and
- * g_j = sum_i u_i.(r_i - r_j)/|r_i - r_j|^3; the adjoint stage 2 reverses the state
- * (r_k = r_{k+1} - T v_{k+1}, v_k = v_{k+1} - T a_k, FP64), updates
+ * kernel forms h = J_A(r_k)^T u and g_j = sum_i u_i.(r_i - r_j)/|r_i - r_j|^3, and
+ * recomputes a_k = A(r_k) (stage 1) unless a->a_in holds it; the adjoint stage 2
+ * reverses the state (r_k = r_{k+1} - T v_{k+1}, v_k = v_{k+1} - T a_k, FP64), updates
  * gr += T h, gv = u, ggm -= T g, and prepares the next step.
  * Transposes universe_base.step_stage1/step_stage2 (_base_.py:147-156); no
  * counterpart in the reference (it has no gradients).

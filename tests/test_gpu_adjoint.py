@@ -36,15 +36,17 @@ def relerr(a, b):
 
 
 @pytest.mark.parametrize('pairs', [False, True])
-def test_single_step_against_oracle_vjp(gpu, pairs):
+@pytest.mark.parametrize('store_a', [False, True])
+def test_single_step_against_oracle_vjp(gpu, pairs, store_a):
     """Both backward pair kernels: every ordered pair, and each unordered pair once
-    (700 bodies = 3 row blocks of the unique-pair plan, so column slots are used)."""
+    (700 bodies = 3 row blocks of the unique-pair plan, so column slots are used), each
+    recomputing the accelerations or taking the forward's (store_a)."""
     n = 700
     r, v, m = compact(n, 3)
     rng = np.random.default_rng(1)
     c = rng.normal(size=(n, 3))
-    ro = Rollout([n], T, 1, every=1, adj_pairs=pairs)
-    assert ro.adj.pairs == pairs
+    ro = Rollout([n], T, 1, every=1, adj_pairs=pairs, store_a=store_a)
+    assert ro.adj.pairs == pairs and ro.store_a == store_a
     dev = torch.device('cuda')
     rK, vK = ro.forward(torch.tensor(r, device=dev), torch.tensor(v, device=dev),
                         torch.tensor(G_DEFAULT * m, device=dev))
@@ -63,9 +65,10 @@ def test_single_step_against_oracle_vjp(gpu, pairs):
     assert np.max(np.abs(v_rev.cpu().numpy() - v)) <= 1e-15 + 1e-9 * np.max(np.abs(v))
 
 
-@pytest.mark.parametrize('every,n,pairs', [(1, 192, None), (8, 192, None), (40, 192, None),
-                                           (8, 600, True)])
-def test_rollout_against_torch_autograd(gpu, every, n, pairs):
+@pytest.mark.parametrize('every,n,pairs,store_a', [(1, 192, None, None), (8, 192, None, None),
+                                                   (40, 192, None, False), (8, 600, True, None),
+                                                   (8, 600, True, False), (13, 600, True, True)])
+def test_rollout_against_torch_autograd(gpu, every, n, pairs, store_a):
     steps = 40
     r, v, m = compact(n, 5)
     tgt = r + np.random.default_rng(2).normal(scale=1.0, size=r.shape)
@@ -81,7 +84,8 @@ def test_rollout_against_torch_autograd(gpu, every, n, pairs):
         loss.backward()
         return [x.grad.cpu().numpy() for x in (r0, v0, mm)], float(loss)
 
-    ro = Rollout([n], T, steps, every, adj_pairs=pairs) if pairs is not None else None
+    ro = (Rollout([n], T, steps, every, adj_pairs=pairs, store_a=store_a)
+          if pairs is not None or store_a is not None else None)
     ours, l1 = grads(lambda a, b, c: rollout(a, b, c, G, T, steps, every=every, ro=ro))
     ref, l2 = grads(lambda a, b, c: torch_reference_rollout(a, b, c, G, T, steps))
     assert abs(l1 - l2) <= 1e-6 * abs(l2)

@@ -260,6 +260,58 @@ def test_batched_matches_single(gpu):
         eng.raise_on_device_error()
 
 
+@pytest.mark.parametrize('mode', ['fp32', 'fp32u', 'fp32c', 'fp32cu', 'fp64'])
+def test_empty_and_ragged_batches(gpu, mode):
+    """Universes without bodies anywhere in a batch (first, between, last) take no rows
+    and leave the others' answers unchanged; batches of nothing but empty universes step
+    without a launch error (stage 1 and stage 2 then launch nothing)."""
+    sizes = [0, 5, 0, 1, 300, 0, 2, 0]
+    parts = [uniform_cube(n, seed=110 + i) for i, n in enumerate(sizes)]
+    r = np.concatenate([p[0] for p in parts])
+    v = np.concatenate([p[1] for p in parts])
+    m = np.concatenate([p[2] for p in parts])
+    eng = Engine(sizes, 1e3, mode=mode)
+    eng.set_state(r, v, G_DEFAULT * m)
+    a = eng.forces().cpu().numpy()
+    eng.raise_on_device_error()
+    for u, n in enumerate(sizes):
+        sl = eng.universe_slice(u)
+        assert a[sl].shape[0] == n
+        if n < 2:
+            assert np.all(a[sl] == 0.0)
+            continue
+        ref = oracle_accel(mode, parts[u][0], parts[u][2], G_DEFAULT)
+        assert oracle.rel_err_per_body(a[sl], ref).max() < TOL[mode], (mode, u)
+    eng.step(2)
+    out = eng.energy(G_DEFAULT)
+    assert np.all(np.isfinite(out))
+    eng.raise_on_device_error()
+    for empty in ([0], [0, 0, 0]):
+        e = Engine(empty, 1e3, mode=mode)
+        e.set_state(np.zeros((0, 3)), np.zeros((0, 3)), np.zeros(0))
+        assert e.forces().shape[0] == 0
+        e.step(2)
+        torch.cuda.synchronize()
+        e.raise_on_device_error()
+
+
+@pytest.mark.parametrize('mode', ['fp32u', 'fp32'])
+def test_maximum_size_2_20(gpu, mode):
+    """N = 2^20 bodies in one universe (one step is 1.1e12 interactions; the unique-pair
+    plan holds ~525k partial-sum slots): sampled bodies against the FP64 oracle, the
+    total momentum change, and determinism of a repeated evaluation on those bodies."""
+    n = 1 << 20
+    r, v, m = uniform_cube(n, seed=4)
+    rows = np.random.default_rng(20).choice(n, 48, replace=False)
+    a, eng = engine_forces(mode, r, v, m)
+    ref = oracle_accel(mode, r, m, G_DEFAULT, rows=rows)
+    assert oracle.rel_err_per_body(a[rows], ref).max() < TOL[mode]
+    assert np.all(np.isfinite(a))
+    p = (m[:, None] * a).sum(0)
+    assert np.linalg.norm(p) < 1e-5 * (m * np.linalg.norm(a, axis=1)).sum()
+    assert np.array_equal(eng.forces().cpu().numpy()[rows], a[rows])
+
+
 def test_energy_momentum_fp64(gpu):
     """Energy and momentum of every universe of a batch against the FP64 oracle."""
     sizes = [2, 300, 1500, 77]
