@@ -72,6 +72,8 @@ def parse():
     ap.add_argument('--profile-all', action='store_true',
                     help='with --profile: also run steps, the energy diagnostic and adjoint '
                          'steps (for captures of those kernels)')
+    ap.add_argument('--adjoint-n', type=int, default=4096,
+                    help='bodies of the adjoint workload (1000 steps, checkpoint every 32)')
     ap.add_argument('--tile', default=None,
                     help='force the stage-1 tile as bpt,threads,jtile (default: autotuned)')
     a = ap.parse_args()
@@ -539,7 +541,7 @@ def run_workload(args):
     elif args.workload == 'sweep':
         res = {'sweep': workloads.run_sweep(mode=args.mode, tuner=default_tuner())}
     elif args.workload == 'adjoint':
-        res = workloads.run_adjoint(tuner=default_tuner())
+        res = workloads.run_adjoint(n=args.adjoint_n, tuner=default_tuner())
     elif args.workload == 'adjoint-check':
         res = workloads.run_adjoint_check()
     elif args.workload == 'scenario':
