@@ -350,8 +350,11 @@ def run_ours(args):
             adj.set_state(eng.r[:n], eng.v[:n])
             adj.gr[:n, :3].normal_()
             for _ in range(args.warmup + args.steps):
-                eng.step(1)
+                eng.step(1, write_a=True)
                 eng.energy(G_DEFAULT)
+                # the backward step with the forward's accelerations, then recomputing them
+                adj.prepare()
+                adj.step(a_in=eng.a)
                 adj.prepare()
                 adj.step()
             adj.raise_on_device_error()
