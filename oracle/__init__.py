@@ -100,22 +100,26 @@ def scenario(kind, n, seed, stream, G, params):
     return r, v
 
 
+def load_port(path):
+    """ctypes binding of a build of oracle/ref_port.c."""
+    L = ctypes.CDLL(path)
+    L.port_stage1_rows.argtypes = [_fp, _fp, _fp, _fp, ctypes.c_float, ctypes.c_int64,
+                                   ctypes.c_int64, ctypes.c_int64, _fp, _fp, _fp, _fp,
+                                   ctypes.c_int]
+    L.port_stage1_rows.restype = None
+    L.port_segments.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+                                ctypes.c_int, _i64p]
+    L.port_segments.restype = None
+    L.port_stage2.argtypes = [_fp] * 9 + [ctypes.c_float, ctypes.c_int64]
+    L.port_stage2.restype = None
+    return L
+
+
 def port_lib():
     """The portable CPU-baseline library (built on first use)."""
     global _PORT
     if _PORT is None:
-        path = _build.build_port()
-        L = ctypes.CDLL(path)
-        L.port_stage1_rows.argtypes = [_fp, _fp, _fp, _fp, ctypes.c_float, ctypes.c_int64,
-                                       ctypes.c_int64, ctypes.c_int64, _fp, _fp, _fp, _fp,
-                                       ctypes.c_int]
-        L.port_stage1_rows.restype = None
-        L.port_segments.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
-                                    ctypes.c_int, _i64p]
-        L.port_segments.restype = None
-        L.port_stage2.argtypes = [_fp] * 9 + [ctypes.c_float, ctypes.c_int64]
-        L.port_stage2.restype = None
-        _PORT = L
+        _PORT = load_port(_build.build_port())
     return _PORT
 
 
@@ -272,7 +276,8 @@ def vjp_fp64(r, m, G, u, threads=None):
 class PortStage1:
     """FP32 SoA buffers + scratch for ``port_stage1_rows`` (c4a/cy4 design)."""
 
-    def __init__(self, r, m, G, threads=None):
+    def __init__(self, r, m, G, threads=None, lib=None):
+        self.lib = lib  # another build of ref_port.c (load_port), default port_lib()
         r = np.asarray(r, dtype=np.float64).reshape(-1, 3)
         self.n = r.shape[0]
         self.threads = int(threads or default_threads())
@@ -286,7 +291,7 @@ class PortStage1:
 
     def run(self, row0=0, row1=None):
         row1 = self.n if row1 is None else row1
-        port_lib().port_stage1_rows(
+        (self.lib or port_lib()).port_stage1_rows(
             _ptr(self.x, _fp), _ptr(self.y, _fp), _ptr(self.z, _fp), _ptr(self.m, _fp),
             self.G, self.n, int(row0), int(row1),
             _ptr(self.a[0], _fp), _ptr(self.a[1], _fp), _ptr(self.a[2], _fp),

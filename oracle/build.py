@@ -60,6 +60,28 @@ def build_port(force=False):
     return out
 
 
+def reference_flags():
+    """The reference's C optimisation flags (setup.py:103-118) on this host."""
+    flags = ['-O3', '-ffast-math']
+    if platform.machine() in ('x86_64', 'AMD64'):
+        flags += ['-march=native', '-mtune=native', '-mfpmath=sse']
+    return flags
+
+
+def build_port_reference_flags(force=False):
+    """ref_port.c compiled with exactly the reference's flags on this host (x86:
+    -march=native etc.), into oracle/_ref/, for a like-for-like comparison with the
+    reference's own C kernel; the timed baseline uses the portable build_port()."""
+    refdir = os.path.join(HERE, '_ref')
+    os.makedirs(refdir, exist_ok=True)
+    out = os.path.join(refdir, 'libport_refflags.so')
+    src = os.path.join(HERE, 'ref_port.c')
+    if force or not _newer(out, src):
+        _run(['gcc'] + reference_flags() + ['-fPIC', '-shared', '-fopenmp', '-std=gnu11',
+                                            src, '-o', out, '-lm'])
+    return out
+
+
 def reference_present():
     return os.path.isfile(os.path.join(REF_KERNEL, '_base_.py'))
 
@@ -78,9 +100,7 @@ def build_reference(force=False):
     lib1_out = os.path.join(refdir, 'lib1.so')
     try:
         if force or not _newer(lib1_out, lib1_src):
-            flags = ['-std=gnu11', '-fPIC', '-O3', '-ffast-math', '-Wall']
-            if platform.machine() in ('x86_64', 'AMD64'):
-                flags += ['-march=native', '-mtune=native', '-mfpmath=sse']
+            flags = ['-std=gnu11', '-fPIC', '-Wall'] + reference_flags()
             _run(['gcc'] + flags + ['-shared', lib1_src, '-o', lib1_out, '-lm'])
         result['lib1'] = lib1_out
     except (subprocess.CalledProcessError, OSError) as e:
