@@ -4,12 +4,14 @@
 runs ``steps`` GB300 steps (FP32 stage 1, FP64 stage 2) and keeps the FP64 state at
 the start of every ``every``-step segment; its backward sweeps the segments from last
 to first.  Each segment starts from the exact stored state at its end and reverses the
-update step by step in FP64, while the adjoint pair kernel applies the transposed
-stage 2 and stage 1 at each reconstructed position (see csrc/adjoint.cu).  The
-reversal uses the forward's own accelerations of each step where they are kept
-(``store_a``: steps x 32 bytes per body), else the pair kernel recomputes stage 1 as
-well.  Gradients are returned for the initial positions, velocities and masses.
-Memory: one FP64 state per segment, plus the kept accelerations.
+update step by step in FP64, while the adjoint pair kernel recomputes stage 1 at each
+reconstructed position and applies the transposed stage 2 and stage 1 (see
+csrc/adjoint.cu).  Gradients are returned for the initial positions, velocities and
+masses.  Memory: one FP64 state per segment, no per-step storage.
+
+Option ``store_a`` trades memory for time: the forward keeps every step's FP64
+accelerations (steps x 32 bytes per body), the reversal uses them and the pair kernel
+forms only the transposed terms, without recomputing stage 1.
 """
 
 import ctypes
@@ -151,14 +153,16 @@ class AdjointEngine:
 class Rollout:
     """Forward engine + adjoint engine for one batch of universes (reusable).
 
-    store_a: keep the forward's FP64 accelerations of every step (steps x n_bodies x 32
-    bytes) so that the backward pair kernel forms only J^T u and the mass term instead
-    of recomputing stage 1 as well (about 15 % fewer operations per pair, 4 slot
-    components instead of 7), and the reversal v_k = v_{k+1} - T a_k uses the very a_k
-    of the forward.  None: when that fits the slot budget (engine.slot_budget_bytes)."""
+    store_a: False (default) -- checkpoints only; the backward pair kernel recomputes
+    stage 1 at every reconstructed position.  True -- the forward also keeps its FP64
+    accelerations of every step (steps x n_bodies x 32 bytes), so that the backward pair
+    kernel forms only J^T u and the mass term (about 15 % fewer operations per pair, 4
+    slot components instead of 7) and the reversal v_k = v_{k+1} - T a_k uses the very
+    a_k of the forward.  'auto': True when that fits the slot budget
+    (engine.slot_budget_bytes)."""
 
     def __init__(self, sizes, T, steps, every=32, device=None, fwd_tile=None, tuner=None,
-                 mode=None, graphs=True, adj_pairs=None, store_a=None):
+                 mode=None, graphs=True, adj_pairs=None, store_a=False):
         self.sizes = [int(n) for n in sizes]
         self.T = float(T)
         self.steps = int(steps)
@@ -183,7 +187,7 @@ class Rollout:
         self.ck_r = torch.zeros((nseg + 1, n, 4), dtype=torch.float64, device=self.fwd.device)
         self.ck_v = torch.zeros_like(self.ck_r)
         self.checkpoints = []
-        if store_a is None:
+        if store_a == 'auto':
             from .engine import slot_budget_bytes
             store_a = self.steps * max(n, 1) * 32 <= slot_budget_bytes(self.fwd.device)
         self.store_a = bool(store_a)

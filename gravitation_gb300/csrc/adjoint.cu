@@ -214,17 +214,41 @@ __global__ void __launch_bounds__(AS2_THREADS) adjoint_stage2_kernel(const grav_
 	}
 	const int64_t row = U.body_off + il;
 	const double T = U.T;
+	// Split rows (ATPR >= 4) spread the row's FP64 work over its lanes: lane c < 3 takes
+	// component c of r, v, gr, gv (and of a and h), lane 3 the mass terms.  GB300 issues an
+	// FP64 warp instruction at the same cost whatever the number of active lanes, so this
+	// cuts a warp's FP64 instructions about 3x against one lane doing the whole row.  With
+	// one lane per row (ATPR = 1) every lane already holds a row of its own.
+	constexpr bool SPLIT = ATPR >= 4;
 	arow4* rr = reinterpret_cast<arow4*>(b.r);
 	arow4* vv = reinterpret_cast<arow4*>(b.v);
 	arow4* grr = reinterpret_cast<arow4*>(gr);
 	arow4* gvv = reinterpret_cast<arow4*>(gv);
-	// lane 0 owns the row's update: its loads go out before the slot loads
+	double* rd = static_cast<double*>(b.r);
+	double* vd = static_cast<double*>(b.v);
+	const int64_t e = 4 * row + (p < 3 ? p : 3);  // this lane's component (SPLIT)
+	// the row's state goes out before the slot loads
 	arow4 r = {0.0, 0.0, 0.0, 0.0}, v = r, a_gr = r, a_gv = r, acc = r;
-	if (p == 0) {
+	double rc = 0.0, vc = 0.0, grc = 0.0, gvc = 0.0, ac = 0.0;
+	double gm_acc = 0.0;
+	if (SPLIT) {
+		if (p < 4) {
+			rc = rd[e];  // x, y, z or G*m
+			if (p < 3) {
+				vc = vd[e];
+				grc = gr[e];
+				gvc = gv[e];
+				if ((flags & ADJ_STEP) && a_in) ac = __ldcs(a_in + e);  // read once: evict-first
+			} else if (flags & ADJ_STEP) {
+				gm_acc = ggm[row];
+			}
+		}
+	} else if (p == 0) {
 		r = rr[row];
 		v = vv[row];
 		a_gr = grr[row];
 		a_gv = gvv[row];
+		if (flags & ADJ_STEP) gm_acc = ggm[row];
 		if ((flags & ADJ_STEP) && a_in) {  // read once: evict-first
 			const double2* ai = reinterpret_cast<const double2*>(a_in) + 2 * row;
 			const double2 axy = __ldcs(ai), az = __ldcs(ai + 1);
@@ -232,15 +256,15 @@ __global__ void __launch_bounds__(AS2_THREADS) adjoint_stage2_kernel(const grav_
 		}
 	}
 
-	double s[NC];
+	float h[NC], l[NC];
 #pragma unroll
-	for (int c = 0; c < NC; ++c) s[c] = 0.0;
+	for (int c = 0; c < NC; ++c) h[c] = l[c] = 0.f;
 	if (flags & ADJ_STEP) {
 		// slots p, p + ATPR, ... hold FP32 (hi, lo) pairs; they are added in order into
 		// compensated FP32 sums (hi by TwoSum, lo and the errors into l), each round
-		// issuing all its loads first (the ones past the end are skipped), combined
-		// across the lanes by a TwoSum butterfly and widened once: no FP64 arithmetic
-		// per slot (GB300 runs FP64 at ~1/64 of the FP32 rate)
+		// issuing all its loads first, and combined across the lanes by a TwoSum butterfly
+		// that leaves every lane with the same bits: no FP64 arithmetic per slot (GB300
+		// runs FP64 at ~1/64 of the FP32 rate)
 		constexpr int SLOT_BATCH = NC == 4 ? 6 : 4;
 		const int64_t stride = NC * static_cast<int64_t>(IT);  // 8-byte entries per slot
 		// unique-pair plans: the last (row block index) slots of a segment are column
@@ -248,51 +272,85 @@ __global__ void __launch_bounds__(AS2_THREADS) adjoint_stage2_kernel(const grav_
 		const int nrow = b.mode == GRAV_MODE_FP32U ? S.nslots - S.il0 / IT : S.nslots;
 		const float2* part =
 			reinterpret_cast<const float2*>(b.part + static_cast<int64_t>(S.slot_base) * stride) + li;
-		float h[NC], l[NC];
-#pragma unroll
-		for (int c = 0; c < NC; ++c) h[c] = l[c] = 0.f;
-		for (int k = p; k < nrow; k += SLOT_BATCH * ATPR) {
-			const int m = min(SLOT_BATCH, (nrow - k + ATPR - 1) / ATPR);
-			float2 q[SLOT_BATCH][NC];
-#pragma unroll
-			for (int j = 0; j < SLOT_BATCH; ++j)
-				if (j < m) {
-#pragma unroll
-					for (int c = 0; c < NC; ++c) q[j][c] = __ldg(part + (k + j * ATPR) * stride + c * IT);
-				}
-#pragma unroll
-			for (int j = 0; j < SLOT_BATCH; ++j)
-				if (j < m) {
-#pragma unroll
-					for (int c = 0; c < NC; ++c) {
-						two_sum_acc(h[c], l[c], q[j][c].x);
-						l[c] += q[j][c].y;
-					}
-				}
-		}
 		const float* cpart =
 			reinterpret_cast<const float*>(b.part + static_cast<int64_t>(S.slot_base) * stride) + li;
-		for (int k = nrow + p; k < S.nslots; k += SLOT_BATCH * ATPR) {
-			float q[SLOT_BATCH][NC];
+		// row and column slots share one index space and one round of loads per batch
+		// (slots past the end read as 0, added exactly)
+		for (int k = p; k < S.nslots; k += SLOT_BATCH * ATPR) {
+			float2 q[SLOT_BATCH][NC];
+#pragma unroll
+			for (int j = 0; j < SLOT_BATCH; ++j) {
+				const int kk = k + j * ATPR;
+				if (kk < nrow) {
+#pragma unroll
+					for (int c = 0; c < NC; ++c) q[j][c] = __ldg(part + kk * stride + c * IT);
+				} else if (kk < S.nslots) {
+#pragma unroll
+					for (int c = 0; c < NC; ++c)
+						q[j][c] = make_float2(__ldg(cpart + kk * 2 * stride + c * IT), 0.f);
+				} else {
+#pragma unroll
+					for (int c = 0; c < NC; ++c) q[j][c] = make_float2(0.f, 0.f);
+				}
+			}
 #pragma unroll
 			for (int j = 0; j < SLOT_BATCH; ++j)
 #pragma unroll
-				for (int c = 0; c < NC; ++c)  // loads past the end read as 0, added exactly
-					q[j][c] = (k + j * ATPR < S.nslots) ? __ldg(cpart + (k + j * ATPR) * 2 * stride + c * IT)
-					                                  : 0.f;
-#pragma unroll
-			for (int j = 0; j < SLOT_BATCH; ++j)
-#pragma unroll
-				for (int c = 0; c < NC; ++c) two_sum_acc(h[c], l[c], q[j][c]);
+				for (int c = 0; c < NC; ++c) {
+					two_sum_acc(h[c], l[c], q[j][c].x);
+					l[c] += q[j][c].y;
+				}
 		}
 #pragma unroll
-		for (int c = 0; c < NC; ++c) {
-			group_sum_pair<ATPR>(h[c], l[c], gmask);
-			s[c] = static_cast<double>(h[c]) + static_cast<double>(l[c]);
-		}
+		for (int c = 0; c < NC; ++c) group_sum_pair<ATPR>(h[c], l[c], gmask);
 	}
-	if (p != 0) return;
 
+	if (SPLIT) {
+		if (p >= 4) return;
+		float* posf = reinterpret_cast<float*>(pos) + 4 * g + p;
+		float* uposf = reinterpret_cast<float*>(upos) + 4 * g + p;
+		if (p == 3) {  // mass terms
+			if (flags & ADJ_STEP)
+				ggm[row] = gm_acc - T * (static_cast<double>(h[G0]) + static_cast<double>(l[G0]));
+			if (flags & ADJ_PREPARE) {
+				*posf = __double2float_rn(rc);
+				*uposf = 0.f;
+			}
+			return;
+		}
+		if (flags & ADJ_STEP) {
+			// this lane's component of a (recomputed, NC = 7 without a_in) and of h
+			const int ca = p, ch = H0 + p;
+			const float a_h = ca == 0 ? h[0] : (ca == 1 ? h[1] : h[2]);
+			const float a_l = ca == 0 ? l[0] : (ca == 1 ? l[1] : l[2]);
+			const float h_h = ch == H0 ? h[H0] : (ch == H0 + 1 ? h[H0 + 1] : h[H0 + 2]);
+			const float h_l = ch == H0 ? l[H0] : (ch == H0 + 1 ? l[H0 + 1] : l[H0 + 2]);
+			if (NC == 7 && !a_in) ac = static_cast<double>(a_h) + static_cast<double>(a_l);
+			const double hc = static_cast<double>(h_h) + static_cast<double>(h_l);
+			// reverse the forward update: r_k = r_{k+1} - T v_{k+1}; v_k = v_{k+1} - T a_k
+			rc = __dsub_rn(rc, __dmul_rn(vc, T));
+			vc = __dsub_rn(vc, __dmul_rn(ac, T));
+			// gradients
+			const double uc = gvc + T * grc;
+			grc += T * hc;
+			gvc = uc;
+			rd[e] = rc;
+			vd[e] = vc;
+			gr[e] = grc;
+			gv[e] = gvc;
+		}
+		if (flags & ADJ_PREPARE) {
+			// position of the next backward step and the u it contracts with
+			*posf = __double2float_rn(__dsub_rn(rc, __dmul_rn(vc, T)));
+			*uposf = __double2float_rn(gvc + T * grc);
+		}
+		return;
+	}
+
+	if (p != 0) return;
+	double s[NC];
+#pragma unroll
+	for (int c = 0; c < NC; ++c) s[c] = static_cast<double>(h[c]) + static_cast<double>(l[c]);
 	if (flags & ADJ_STEP) {
 		// reverse the forward update: r_k = r_{k+1} - T v_{k+1}; v_k = v_{k+1} - T a_k
 		if (NC == 7 && !a_in) acc = arow4{s[0], s[1], s[2], 0.0};
@@ -310,7 +368,7 @@ __global__ void __launch_bounds__(AS2_THREADS) adjoint_stage2_kernel(const grav_
 		a_gv.x = ux;
 		a_gv.y = uy;
 		a_gv.z = uz;
-		ggm[row] -= T * s[G0];
+		ggm[row] = gm_acc - T * s[G0];
 		rr[row] = r;
 		vv[row] = v;
 		grr[row] = a_gr;
