@@ -64,7 +64,7 @@ def parse():
     ap.add_argument('--no-adjoint', action='store_true')
     ap.add_argument('--workload', default=None,
                     choices=('precision', 'sweep', 'adjoint', 'adjoint-check', 'scenario',
-                             'frontend'),
+                             'frontend', 'batched'),
                     help='run one secondary workload instead of the headline step')
     ap.add_argument('--profile', action='store_true',
                     help='only set up the workload and run --steps stage-1 launches '
@@ -528,7 +528,9 @@ def read_profile_traffic(mode):
 
 def run_workload(args):
     """Secondary workloads, one JSON line each: precision (Plummer pair, 3 modes,
-    energy/momentum drift), sweep (N = 2^4 .. 2^17), adjoint (forward+adjoint)."""
+    energy/momentum drift), sweep (N = 2^4 .. 2^17), adjoint (forward+adjoint), batched
+    (256 universes vs the per-universe loop; with --profile the batched step alone),
+    scenario generation and the reference's benchmark protocol through gb1 (frontend)."""
     import torch
     torch.cuda.set_device(0)
     from gravitation_gb300 import workloads
@@ -551,6 +553,24 @@ def run_workload(args):
         res = workloads.run_generate(hbm_gbs=measured_peaks().get('hbm_gbs'))
     elif args.workload == 'frontend':
         res = workloads.run_frontend()
+    elif args.workload == 'batched':
+        if args.profile:
+            # the batched step alone, with a fixed tile (for ncu captures)
+            from gravitation_gb300 import _lib
+            from gravitation_gb300.engine import Engine
+            from gravitation_gb300.scenarios import T_DEFAULT
+            sizes, states = workloads.batch_universes(256, 1)
+            bpt, thr, jt = (int(x) for x in (args.tile or '4,128,128').split(','))
+            eng = Engine(sizes, T_DEFAULT, mode=args.mode, tile=_lib.Tile(bpt, thr, jt, 0))
+            eng.set_state(np.concatenate([x[0] for x in states]),
+                          np.concatenate([x[1] for x in states]),
+                          workloads.G_DEFAULT * np.concatenate([x[2] for x in states]))
+            eng.step(args.warmup + args.steps)
+            torch.cuda.synchronize()
+            eng.raise_on_device_error()
+            return 0
+        res = workloads.run_batched(steps=100, warmup=args.warmup, mode=args.mode,
+                                    tuner=default_tuner())
     else:
         raise SystemExit('unknown workload %r' % args.workload)
     res['workload_name'] = args.workload
