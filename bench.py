@@ -216,6 +216,19 @@ def workload_name(n, mode):
 
 # ---- CPU baseline (the reference's CPU design, restated portably) -------------------------
 
+def cpu_model():
+    """The host CPU's model name (lscpu), for the CPU-baseline record."""
+    try:
+        out = subprocess.run(['lscpu'], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith('model name'):
+                return line.split(':', 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
 def cpu_baseline_run(n, seed, target_s, runs=3):
     """Time the unique-pair OpenMP stage 1 (oracle/ref_port.c) on rows [0, k) of the pair
     triangle of the workload, k sized for about target_s seconds; best of `runs`.
@@ -268,7 +281,7 @@ def run_reference(args):
                    'timed': 'stage 1 (unique pairs, FP32); the O(N) stage 2 is under 1e-4 '
                             'of a CPU step at this size and not timed'},
         'cpu_baseline': {'value': value, 'unit': UNIT, 'cores': threads, 'kind': 'port',
-                         'sample': sample},
+                         'cpu_model': cpu_model(), 'sample': sample},
         'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
         'note': ('oracle/ref_port.c restates the reference c4a design (unique pairs, OpenMP '
                  'row segments balanced by pair count, private accumulators, serial '
@@ -431,7 +444,8 @@ def run_ours(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cv, threads, sample = cpu_baseline_run(n, 0, args.cpu_seconds)
-        cpu = {'value': cv, 'unit': UNIT, 'cores': threads, 'kind': 'port', 'sample': sample}
+        cpu = {'value': cv, 'unit': UNIT, 'cores': threads, 'kind': 'port',
+               'cpu_model': cpu_model(), 'sample': sample}
 
     if rank != 0:
         return 0
@@ -545,6 +559,12 @@ def run_workload(args):
                                       steps=args.steps, check=check)
     elif args.workload == 'sweep':
         res = {'sweep': workloads.run_sweep(mode=args.mode, tuner=default_tuner())}
+        # the CPU baseline (the reference's design, restated portably) at every size
+        for row in res['sweep']:
+            cv, threads, sample = cpu_baseline_run(row['n'], 0, 0.5)
+            row['cpu_baseline'] = {'value': cv, 'cores': threads, 'sample': sample}
+            row['gpu_over_cpu'] = row['interactions_per_s'] / cv
+        res['cpu_model'] = cpu_model()
     elif args.workload == 'adjoint':
         res = workloads.run_adjoint(n=args.adjoint_n, tuner=default_tuner())
     elif args.workload == 'adjoint-check':
