@@ -17,8 +17,9 @@ Behaviour seen from the front end (README.md:50, worker.py:119-136):
 
 Kernel options (keyword arguments of the constructor, kept in self._meta):
   precision  'fp32' | 'fp32u' | 'fp32c' | 'fp32cu' | 'fp64'   default from dtype:
-             'float32' -> fp32 below 8192 bodies, fp32u from there on; 'float64' ->
-             fp64.  fp32/fp32u share the FP32 arithmetic (fp32u visits each pair
+             'float32' -> fp32 below 8192 bodies, fp32u from there on while its
+             partial-sum slots fit an eighth of the GPU's memory (~1.7 M bodies);
+             'float64' -> fp64.  fp32/fp32u share the FP32 arithmetic (fp32u visits each pair
              once); fp32c/fp32cu add the low parts of the positions (separations
              exact to FP32 precision anywhere in space)
   host_sync  'full' (upload + download every step) | 'pull' (download only) |
