@@ -68,6 +68,97 @@ def test_reference_inventory_discovers_gb1(tmp_path):
     assert 'OK' in res.stdout
 
 
+_FAKE_H5PY = '''
+"""In-memory stand-in for the h5py calls of gravitation/lib/simulation.py (File,
+create_group, create_dataset, attrs, item access), persisted with pickle so that a file
+written by one call can be read by the next.  Test double only: h5py is absent here."""
+import os, pickle
+import numpy as np
+
+class _Group(dict):
+    def __init__(self):
+        super().__init__()
+        self.attrs = {}
+    def create_group(self, name):
+        if name in self:
+            raise ValueError('group %s exists' % name)
+        self[name] = _Group()
+        return self[name]
+    def create_dataset(self, name, shape, dtype):
+        self[name] = np.zeros(shape, dtype=np.dtype(dtype))
+        return self[name]
+
+class File(_Group):
+    def __init__(self, fn, mode='r'):
+        super().__init__()
+        self._fn, self._mode = fn, mode
+        if os.path.exists(fn):
+            with open(fn, 'rb') as f:
+                self.update(pickle.load(f))
+        elif mode == 'r':
+            raise OSError(fn)
+    def close(self):
+        if self._mode != 'r':
+            with open(self._fn, 'wb') as f:
+                pickle.dump(dict(self), f)
+'''
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_SRC), reason='reference tree not present')
+def test_reference_store_load_with_gb1(tmp_path):
+    """The reference's own store_simulation / load_simulation (simulation.py:186-258,
+    the worker's snapshot path, worker.py:138-155) run on gb1 universes: the state
+    model they read and write (pm._name, pm._r, pm._v, pm._m and the universe's scale,
+    time step and G attributes) is the reference's.  h5py itself is absent on both hosts,
+    so an in-memory stand-in takes its place; the HDF5 file format is not exercised.  The
+    reference's store also needs numpy's chararray, which numpy 2 keeps under np.char."""
+    src = tmp_path / 'src'
+    shutil.copytree(os.path.join(REF_SRC, 'gravitation'), src / 'gravitation',
+                    ignore=shutil.ignore_patterns('__pycache__', '*.so'))
+    shutil.copytree(GB1, src / 'gravitation' / 'kernel' / 'gb1',
+                    ignore=shutil.ignore_patterns('__pycache__'))
+    fake = tmp_path / 'fake'
+    fake.mkdir()
+    (fake / 'h5py.py').write_text(_FAKE_H5PY)
+    script = textwrap.dedent('''
+        import sys, warnings
+        warnings.simplefilter("ignore", DeprecationWarning)
+        sys.path[:0] = [%r, %r, %r]
+        import numpy as np
+        if not hasattr(np, "chararray"):
+            # simulation.py:241 calls np.chararray, which numpy 2 moved to np.char
+            np.chararray = np.char.chararray
+        from gravitation.lib.load import inventory
+        from gravitation.lib.simulation import store_simulation, load_simulation
+        k = inventory["gb1"]
+        k.load_meta()
+        k.load_module()
+        cls = k.get_class()
+        rng = np.random.default_rng(5)
+        u = cls(T=1.5e3, scale_m=1e-30, scale_r=1e-10, dtype="float32", t=7.0)
+        for i in range(50):
+            u.add_object(name="body %%d" %% i, r=list(rng.uniform(-1e12, 1e12, 3)),
+                         v=list(rng.normal(0, 1e3, 3)), m=float(rng.uniform(1e29, 1e31)))
+        fn = %r
+        store_simulation(u, fn, "kernel=gb1;len=50;step=0")
+        store_simulation(u, fn, "kernel=gb1;len=50;step=1")
+        w = load_simulation(cls, fn, "kernel=gb1;len=50;step=1")
+        assert type(w) is cls and len(w) == 50
+        assert w._G == u._G and w._T == u._T and w._t == u._t
+        assert w._scale_m == u._scale_m and w._scale_r == u._scale_r and w._dtype == u._dtype
+        for a, b in zip(u, w):
+            assert a._name == b._name
+            # the store keeps the universe's dtype (float32 here), as the reference does
+            assert np.allclose(np.float32(a._r), b._r, rtol=0) and np.float32(a._m) == b._m
+            assert np.allclose(np.float32(a._v), b._v, rtol=0)
+        print("OK")
+    ''' % (str(fake), str(src), ROOT, str(tmp_path / 'sim.h5')))
+    res = subprocess.run([sys.executable, '-c', script], capture_output=True, text=True,
+                         timeout=300)
+    assert res.returncode == 0, res.stderr[-2000:]
+    assert 'OK' in res.stdout
+
+
 def _ref_base():
     if not os.path.isdir(REF_SRC):
         pytest.skip('reference tree not present')
