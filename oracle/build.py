@@ -10,6 +10,11 @@ host), compiles the reference's own sources where they lie, into ``oracle/_ref/`
   _ref/lib1.so  -- gravitation/kernel/_lib1_/lib.c (the c1a kernel), with the
                    reference's own flags (setup.py:82-99)
   _ref/cy4/     -- gravitation/kernel/cy4/core.pyx through Cython (setup.py:73-78)
+  _ref/pc2_n<N>.cubin -- the CUDA kernel of gravitation/kernel/pc2.py (its SM string,
+                   pc2.py:59-91), rendered as pc2's start_kernel renders it for FP32 and
+                   N bodies (pc2.py:125-131) and compiled with nvcc for sm_103a: the
+                   reference's own GPU kernel, as a comparator on the GB300 (a cubin is
+                   device code only, so it serves the GPU host as built here)
 The reference's _lib4_/lib.c (c4a/c4b) is not built: it includes x86 SSE headers
 (lib.c:39) and GCC 13 rejects its OpenMP data-sharing clause (lib.c:179-182).
 
@@ -124,9 +129,60 @@ def build_reference(force=False):
     return result
 
 
+PC2_SIZES = (1024, 4096, 16384, 65536)
+
+
+def _pc2_template():
+    """The SM source template of pc2.py (a module-level string), read without importing
+    the module (it needs PyCUDA)."""
+    import ast
+    src = os.path.join(REF_KERNEL, 'pc2.py')
+    tree = ast.parse(open(src).read())
+    for node in tree.body:
+        if isinstance(node, ast.Assign) and any(
+                isinstance(t, ast.Name) and t.id == 'SM' for t in node.targets):
+            return ast.literal_eval(node.value)
+    raise ValueError('no SM template in %s' % src)
+
+
+def build_reference_gpu(sizes=PC2_SIZES, G=6.6740831e-11, force=False):
+    """Compile pc2's kernel for each N in `sizes` (FP32, int32 indices, rsqrtf, the
+    universe's G: the values pc2.py:125-131 formats in) into oracle/_ref/pc2_n<N>.cubin.
+    PyCUDA's SourceModule compiles its source inside extern "C", so the rendered source
+    is wrapped the same way and the kernel keeps its plain name, update_all."""
+    result = {}
+    if not reference_present():
+        return result
+    refdir = os.path.join(HERE, '_ref')
+    os.makedirs(refdir, exist_ok=True)
+    nvcc = shutil.which('nvcc') or '/usr/local/cuda/bin/nvcc'
+    src_py = os.path.join(REF_KERNEL, 'pc2.py')
+    try:
+        tmpl = _pc2_template()
+    except (OSError, ValueError, SyntaxError) as e:
+        return {'pc2': 'unbuildable: %s' % e}
+    for n in sizes:
+        out = os.path.join(refdir, 'pc2_n%d.cubin' % n)
+        try:
+            if force or not _newer(out, src_py):
+                code = tmpl.format(dtype='float', itype='int32', rsqrt='rsqrtf', G=G,
+                                   MASS_LEN=int(n))
+                with tempfile.TemporaryDirectory() as tmp:
+                    cu = os.path.join(tmp, 'pc2_kernel.cu')
+                    with open(cu, 'w') as f:
+                        f.write('extern "C" {\n' + code + '\n}\n')
+                    _run([nvcc, '-cubin', '-O3', '-gencode', 'arch=compute_103a,code=sm_103a',
+                          cu, '-o', out])
+            result['pc2_n%d' % n] = out
+        except (subprocess.CalledProcessError, OSError) as e:
+            result['pc2_n%d' % n] = 'unbuildable: %s' % e
+    return result
+
+
 def build_all(force=False):
     out = {'oracle': build_oracle(force), 'port': build_port(force)}
     out.update(build_reference(force))
+    out.update(build_reference_gpu(force=force))
     return out
 
 

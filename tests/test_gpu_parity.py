@@ -312,6 +312,34 @@ def test_maximum_size_2_20(gpu, mode):
     assert np.array_equal(eng.forces().cpu().numpy()[rows], a[rows])
 
 
+@pytest.mark.parametrize('n', [1024, 4096])
+def test_matches_reference_gpu_kernel(gpu, n):
+    """The reference's own GPU kernel (pc2's update_all, pc2.py:59-91, compiled for
+    sm_103a from the reference's source where the reference tree exists) run on the same
+    GB300 on the same inputs: both are within 1e-5 of the FP64 oracle and within 2e-5 of
+    each other on every body, in fp32 and fp32u."""
+    from oracle import refgpu
+    if not refgpu.available(n):
+        pytest.skip('pc2 cubin not built (the reference tree is not on this host)')
+    r, v, m = uniform_cube(n, seed=0)
+    f32 = dict(dtype=torch.float32, device='cuda')
+    cols = [torch.tensor(r[:, k], **f32) for k in range(3)]
+    acc = [torch.zeros(n, **f32) for _ in range(3)]
+    mm = torch.tensor(m, **f32)
+    k = refgpu.Pc2Kernel(n)
+    k.launch(*(t.data_ptr() for t in cols), *(t.data_ptr() for t in acc), mm.data_ptr(),
+             torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    k.close()
+    a_pc2 = torch.stack(acc, 1).double().cpu().numpy()
+    ref = oracle_accel('fp32', r, m, G_DEFAULT)
+    assert oracle.rel_err_per_body(a_pc2, ref).max() < 1e-5
+    for mode in ('fp32', 'fp32u'):
+        a, _ = engine_forces(mode, r, v, m)
+        assert oracle.rel_err_per_body(a, ref).max() < 1e-5, mode
+        assert oracle.rel_err_per_body(a, a_pc2).max() < 2e-5, mode
+
+
 def test_energy_momentum_fp64(gpu):
     """Energy and momentum of every universe of a batch against the FP64 oracle."""
     sizes = [2, 300, 1500, 77]
