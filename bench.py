@@ -456,7 +456,9 @@ def run_ours(args):
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world,
         'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': max_ms,
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
-        'dtype': 'f32 pair terms, f64 sums and stage 2',
+        'dtype': 'f32',
+        'dtype_detail': ('FP32 pair terms into compensated FP32 (hi, lo) sums; FP64 state and '
+                         'stage 2'),
         'data': 'synthetic (seeded uniform cube; the reference ships no dataset)',
         'config': {'workload': workload_name(n, args.mode),
                    'n': n, 'mode': args.mode,
