@@ -1,7 +1,7 @@
 // energy.cu -- FP64 energy and momentum of every universe of a batch.
 //
 // The reference has no energy diagnostic (an "accuracy" command is a wish, TODO.md:4);
-// the precision modes are judged by the drift of
+// the precision modes are compared by the drift of
 //     E = sum_i 1/2 m_i v_i^2  -  sum_{i<j} G m_i m_j / |r_i - r_j|      and   P = sum_i m_i v_i
 // over a run.  Both are computed in FP64 from the FP64 state with G*m in r[:,3]:
 //   pass 1 (persistent, the stage-1 work list): phi_i = sum_{j!=i} Gm_j / |r_j - r_i|
