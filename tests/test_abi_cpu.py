@@ -247,3 +247,67 @@ def test_pos_and_part_bytes(L):
     assert L.grav_pos_bytes(1, 1024) == 32 * 1024
     assert L.grav_pos_bytes(2, 1024) == 32 * 1024
     assert L.grav_pos_bytes(9, 1024) < 0
+
+
+_C_PROBE = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "gravitation_gb300.h"
+
+int main(void)
+{
+	int32_t n[2] = {1000, 37};
+	double T[2] = {1e3, 2e3};
+	grav_tile t = {4, 128, 128, 456};
+	grav_plan_info info;
+	if (grav_plan(2, n, T, &t, &info, NULL, NULL) != GRAV_OK) {
+		fprintf(stderr, "%s\n", grav_last_error());
+		return 1;
+	}
+	printf("abi %d\n", grav_abi_version());
+	printf("sizes %zu %zu %zu %zu %zu %zu %zu\n", sizeof(grav_univ_desc), sizeof(grav_seg_desc),
+		sizeof(grav_tile), sizeof(grav_plan_info), sizeof(grav_batch), sizeof(grav_adjoint),
+		sizeof(grav_scenario));
+	printf("offsets %zu %zu %zu\n", offsetof(grav_batch, univ), offsetof(grav_batch, err),
+		offsetof(grav_adjoint, a_in));
+	printf("plan %lld %d %d %d\n", (long long)info.n_bodies, info.n_univ, info.n_seg, info.grid);
+	printf("bad %d\n", grav_plan(-1, n, T, &t, &info, NULL, NULL) == GRAV_E_ARG);
+	return 0;
+}
+'''
+
+
+def test_header_compiles_as_c_and_matches_binding(L, tmp_path):
+    """The header is plain C99 (what a cgo or other FFI binding would include): a C program
+    built against it with -Wall -Werror -pedantic links libgravgb300.so, calls the host-only
+    entry points, and reports struct sizes and offsets equal to the ctypes mirror's."""
+    import ctypes
+    import shutil
+    import subprocess
+    if shutil.which('gcc') is None:
+        pytest.skip('gcc not available')
+    src = tmp_path / 'probe.c'
+    src.write_text(_C_PROBE)
+    exe = tmp_path / 'probe'
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    subprocess.run(['gcc', '-std=c99', '-Wall', '-Wextra', '-Werror', '-pedantic',
+                    '-I', os.path.join(ROOT, 'include'), str(src), '-o', str(exe),
+                    '-L', libdir, '-lgravgb300', '-Wl,-rpath,' + libdir], check=True)
+    res = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert res.returncode == 0, res.stderr
+    out = dict(line.split(' ', 1) for line in res.stdout.strip().splitlines())
+    assert int(out['abi']) == _lib.GRAV_ABI_VERSION
+    sizes = [int(x) for x in out['sizes'].split()]
+    assert sizes == [ctypes.sizeof(c) for c in (_lib.UnivDesc, _lib.SegDesc, _lib.Tile,
+                                                _lib.PlanInfo, _lib.Batch, _lib.Adjoint,
+                                                _lib.Scenario)]
+    offs = [int(x) for x in out['offsets'].split()]
+    assert offs == [_lib.Batch.univ.offset, _lib.Batch.err.offset, _lib.Adjoint.a_in.offset]
+    nb, nu, nseg, grid = (int(x) for x in out['plan'].split())
+    info = _lib.PlanInfo()
+    t = _lib.Tile(4, 128, 128, 456)
+    n_arr = (ctypes.c_int32 * 2)(1000, 37)
+    T_arr = (ctypes.c_double * 2)(1e3, 2e3)
+    assert L.grav_plan(2, n_arr, T_arr, ctypes.byref(t), ctypes.byref(info), None, None) == 0
+    assert (nb, nu, nseg, grid) == (info.n_bodies, info.n_univ, info.n_seg, info.grid)
+    assert out['bad'] == '1'
