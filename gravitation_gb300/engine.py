@@ -9,8 +9,9 @@ Layout in HBM (all packed universe after universe):
   r, v     float64 [n_bodies, 4]   (x, y, z, G*m) and (vx, vy, vz, 0); or, after
            bind_host_state, the caller's pinned host tensors of that layout
   pos      padded stage-1 positions: float4 hi (+ float4 lo in fp32c/fp32cu) or double4
-  part     float64 [n_slots, 3, itile]  partial sums written by stage 1 (FP64 row
-           slots; the unique-pair column slots hold FP32 sums in their first half)
+  part     8-byte entries [n_slots, 3, itile]  partial sums written by stage 1: FP32
+           (hi, lo) pairs in the row slots (FP64 values in fp64 mode); the unique-pair
+           column slots hold FP32 sums in their first half
   univ/seg plan tables (grav_univ_desc / grav_seg_desc)
 """
 
