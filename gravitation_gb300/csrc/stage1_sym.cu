@@ -276,6 +276,8 @@ static const Stage1Kernel k_table_sym[] = {
 	GRAV_SYM_ENTRY(4, 4, 256),
 	GRAV_SYM_ENTRY(2, 8, 256),
 	GRAV_SYM_ENTRY(8, 8, 256),
+	GRAV_SYM_ENTRY(8, 4, 128),
+	GRAV_SYM_ENTRY(8, 4, 64),
 	GRAV_SYMC_ENTRY(4, 4, 128),
 	GRAV_SYMC_ENTRY(8, 4, 256),
 	GRAV_SYMC_ENTRY(4, 4, 256),
