@@ -19,8 +19,9 @@
 // block I's units are the j-tiles of blocks J >= I; a j-tile of block I itself is done
 // with every ordered pair, rows only; a j-tile of a block J > I on unique pairs: lane l
 // meets body (l + s) mod 32 of a 32-body chunk at step s while the chunk's column
-// values rotate one lane per step, then warps add them into shared memory and the tile's
-// column sums go, as FP32, to the column slot of (I, J) (block J's last J slots).  Row
+// values rotate one lane per step, then each warp writes them to its own row of a
+// shared-memory buffer, and the tile's column sums (the warps added in a fixed order) go,
+// as FP32, to the column slot of (I, J) (block J's last J slots).  Row
 // sums are compensated FP32 (TwoSum) and go out as FP32 (hi, lo) pairs.  Slot layout
 // [slot][NC][R]: a, h, g (NC = 7) or h, g (NC = 4).
 #include "grav_device.cuh"
@@ -43,7 +44,9 @@ __global__ void __launch_bounds__(32 * W) vjp_sym_kernel(const grav_batch b,
 	constexpr uint32_t TILE_BYTES = JT * sizeof(float4);
 	static_assert(R % JT == 0 && JT % 32 == 0 && (NCH & (NCH - 1)) == 0, "tile shapes");
 	extern __shared__ __align__(128) float4 vs_tiles[];  // [2 buffers][pos, u][JT]
-	__shared__ float colacc[NC][JT];
+	// column sums of a j-tile, one row per warp, added over the warps in a fixed order
+	// at the flush (no shared-memory atomics, whose order would depend on warp timing)
+	__shared__ float colacc[W][NC][JT];
 	__shared__ __align__(8) uint64_t bar[2];
 
 	const int tid = threadIdx.x;
@@ -56,9 +59,6 @@ __global__ void __launch_bounds__(32 * W) vjp_sym_kernel(const grav_batch b,
 	const int64_t ue = (c + 1) * U / G;
 	if (ub >= ue) return;
 
-	for (int i = tid; i < JT; i += T)
-#pragma unroll
-		for (int q = 0; q < NC; ++q) colacc[q][i] = 0.f;
 	if (tid == 0) {
 		mbar_init(&bar[0], 1);
 		mbar_init(&bar[1], 1);
@@ -232,17 +232,18 @@ __global__ void __launch_bounds__(32 * W) vjp_sym_kernel(const grav_batch b,
 					}
 					const int ci0 = ch * 32 + lane;
 					if constexpr (FA) {
-						atomicAdd(&colacc[0][ci0], cax);
-						atomicAdd(&colacc[1][ci0], cay);
-						atomicAdd(&colacc[2][ci0], caz);
+						colacc[warp][0][ci0] = cax;
+						colacc[warp][1][ci0] = cay;
+						colacc[warp][2][ci0] = caz;
 					}
-					atomicAdd(&colacc[H0][ci0], chx);
-					atomicAdd(&colacc[H0 + 1][ci0], chy);
-					atomicAdd(&colacc[H0 + 2][ci0], chz);
-					atomicAdd(&colacc[G0][ci0], cg);
+					colacc[warp][H0][ci0] = chx;
+					colacc[warp][H0 + 1][ci0] = chy;
+					colacc[warp][H0 + 2][ci0] = chz;
+					colacc[warp][G0][ci0] = cg;
 				}
 				__syncthreads();
-				// column sums of this tile -> column slot of (I, J) as FP32, then clear
+				// column sums of this tile -> column slot of (I, J) as FP32, the warps added
+				// in order
 				const int sJ = s + (blkJ - blkI);
 				const grav_seg_desc SJ = b.seg[sJ];
 				const int64_t slot = SJ.slot_base + SJ.nslots - (blkJ - blkI);
@@ -251,8 +252,10 @@ __global__ void __launch_bounds__(32 * W) vjp_sym_kernel(const grav_batch b,
 				for (int i = tid; i < JT; i += T) {
 #pragma unroll
 					for (int q = 0; q < NC; ++q) {
-						out[q * R + i] = colacc[q][i];
-						colacc[q][i] = 0.f;
+						float sq = colacc[0][q][i];
+#pragma unroll
+						for (int w = 1; w < W; ++w) sq += colacc[w][q][i];
+						out[q * R + i] = sq;
 					}
 				}
 			}

@@ -16,13 +16,14 @@
 // each 32-body chunk of the tile, lane l meets body (l + s) mod 32 of the chunk at step
 // s while the chunk's column sums rotate one lane per step (shfl), so after 32 steps
 // every row of the warp has met every body of the chunk once and each lane holds the
-// complete column sum of "its" body.  Warps add their column sums into shared memory
-// (atomics), and the tile's column sums go into the column slot of (I, J): block J's
-// segment lists its row slots first and then one column slot per block I < J (its last
-// J slots), so stage 2 adds them like any partial sums (fixed order, deterministic).
+// complete column sum of "its" body.  Each warp writes its column sums to its own row of
+// a shared-memory buffer, and the tile's column sums (the warps added in a fixed order)
+// go into the column slot of (I, J): block J's segment lists its row slots first and then
+// one column slot per block I < J (its last J slots), so stage 2 adds them like any
+// partial sums (fixed order: the result does not depend on scheduling).
 // Row sums are FP32 per tile, folded into compensated (TwoSum) FP32 hi+lo sums, as in
-// stage1_f32.cu, and go out as FP64; column sums are FP32 per tile and go out as FP32
-// (the first 3R floats of the slot), which stage 2 adds by TwoSum in FP32.
+// stage1_f32.cu, and go out as FP32 (hi, lo) pairs; column sums are FP32 per tile and go
+// out as FP32 (the first 3R floats of the slot), which stage 2 adds by TwoSum in FP32.
 #include "grav_device.cuh"
 
 namespace grav {
@@ -41,7 +42,10 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 	static_assert(R % JT == 0 && JT % 32 == 0, "tile shapes");
 	static_assert(NP == 1 || NP == 2, "one or two position arrays");
 	extern __shared__ __align__(128) float4 sym_tiles[];   // [2 buffers][NP][JT]
-	__shared__ float colacc[3][JT];
+	// column sums of a j-tile, one row per warp: every warp writes each chunk of the tile
+	// once, and the flush adds the warps in a fixed order (no shared-memory atomics, whose
+	// order would depend on warp timing)
+	__shared__ float colacc[W][3][JT];
 	__shared__ __align__(8) uint64_t bar[2];
 
 	const int tid = threadIdx.x;
@@ -54,7 +58,6 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 	const int64_t ue = (c + 1) * U / G;
 	if (ub >= ue) return;
 
-	for (int i = tid; i < JT; i += T) colacc[0][i] = colacc[1][i] = colacc[2][i] = 0.f;
 	if (tid == 0) {
 		mbar_init(&bar[0], 1);
 		mbar_init(&bar[1], 1);
@@ -211,24 +214,30 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 						cy = __shfl_sync(0xffffffffu, cy, src);
 						cz = __shfl_sync(0xffffffffu, cz, src);
 					}
-					atomicAdd(&colacc[0][ch * 32 + lane], cx);
-					atomicAdd(&colacc[1][ch * 32 + lane], cy);
-					atomicAdd(&colacc[2][ch * 32 + lane], cz);
+					colacc[warp][0][ch * 32 + lane] = cx;
+					colacc[warp][1][ch * 32 + lane] = cy;
+					colacc[warp][2][ch * 32 + lane] = cz;
 				}
 				__syncthreads();
-				// column sums of this tile -> column slot of (I, J), then clear.  They are
-				// FP32 sums, so they go out as FP32 (first half of the slot; stage 2
-				// adds them by TwoSum in FP32): half the bytes of an FP64 slot
+				// column sums of this tile -> column slot of (I, J), the warps added in order.
+				// They are FP32 sums, so they go out as FP32 (first half of the slot; stage
+				// 2 adds them by TwoSum in FP32): half the bytes of an FP64 slot
 				const int sJ = s + (blkJ - blkI);
 				const grav_seg_desc SJ = b.seg[sJ];
 				const int64_t slot = SJ.slot_base + SJ.nslots - (blkJ - blkI);
 				float* __restrict__ out = reinterpret_cast<float*>(b.part + slot * 3 * R) +
 					(jt * JT - static_cast<int64_t>(blkJ) * R);
 				for (int i = tid; i < JT; i += T) {
-					out[i] = colacc[0][i];
-					out[R + i] = colacc[1][i];
-					out[2 * R + i] = colacc[2][i];
-					colacc[0][i] = colacc[1][i] = colacc[2][i] = 0.f;
+					float sx = colacc[0][0][i], sy = colacc[0][1][i], sz = colacc[0][2][i];
+#pragma unroll
+					for (int w = 1; w < W; ++w) {
+						sx += colacc[w][0][i];
+						sy += colacc[w][1][i];
+						sz += colacc[w][2][i];
+					}
+					out[i] = sx;
+					out[R + i] = sy;
+					out[2 * R + i] = sz;
 				}
 			}
 #pragma unroll
