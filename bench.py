@@ -3,9 +3,15 @@
 
 Workload (default): one universe of N = 65536 bodies, positions U[-1000,1000]^3,
 velocities N(0,1), masses U[1,100] (seed 0), G = 6.6740831e-11, T = 1e3 -- FP32
-pairwise stage 1 over unique pairs with compensated sums and FP64 stage 2 ("fp32u"
-mode; --mode picks another).  Synthetic data: the reference has no dataset, its own
-scenarios are generated too.
+pairwise stage 1 over unique pairs with compensated sums, near pairs from
+double-single separations, and FP64 stage 2 ("fp32un", the plugin's float32 default at
+this size; --mode picks another).  Synthetic data: the reference has no dataset, its
+own scenarios are generated too.
+
+  accuracy   every body's acceleration in the timed mode against the GPU's FP64 mode on
+             the same FP64 state (max and tail of |a - a64| / |a64| over all N bodies);
+             the FP64 mode itself is checked against the CPU FP64 oracle on sampled
+             bodies in the same run
 
   value      pair interactions per second (N^2 per step), device-timed steps with the
              state resident in HBM; L2 flushed (256 MiB write) between timed steps
@@ -42,8 +48,10 @@ METRIC = ('pair-interactions/s/GPU at N=65536 and fwd+adjoint steps/s at ≤1e-5
 UNIT = 'interactions/s'
 FLOP_PER_INTERACTION = 20
 STAGE1_KERNEL = {'fp32': 'stage1_f32_kernel<FP32>', 'fp32c': 'stage1_f32_kernel<FP32C>',
-                 'fp64': 'stage1_f64_kernel', 'fp32u': 'stage1_sym_kernel<NP=1>',
-                 'fp32cu': 'stage1_sym_kernel<NP=2>'}
+                 'fp32n': 'stage1_f32_kernel<FP32N>', 'fp64': 'stage1_f64_kernel',
+                 'fp32u': 'stage1_sym_kernel<SYM_PLAIN>', 'fp32cu': 'stage1_sym_kernel<SYM_DS>',
+                 'fp32un': 'stage1_sym_kernel<SYM_NEAR>'}
+MODES = ('fp32', 'fp32u', 'fp32n', 'fp32un', 'fp32c', 'fp32cu', 'fp64')
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -54,8 +62,7 @@ def parse():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', choices=('ours', 'reference'), default='ours')
     ap.add_argument('--n', type=int, default=65536)
-    ap.add_argument('--mode', default='fp32u',
-                    choices=('fp32', 'fp32u', 'fp32c', 'fp32cu', 'fp64'))
+    ap.add_argument('--mode', default='fp32un', choices=MODES)
     ap.add_argument('--cpu-seconds', type=float, default=4.0,
                     help='target seconds per CPU-baseline sample run (3 runs)')
     ap.add_argument('--no-cpu', action='store_true')
@@ -315,18 +322,32 @@ def measure_fp32_peak(torch, lib, info, device):
     return 2.0 * fmas / (best * 1e-3)
 
 
-def sampled_errors(eng, r, m, G, rows):
-    """Max relative error of the current forces on `rows` against the FP64 oracle,
-    on the FP32-rounded state (arithmetic) and on the FP64 state."""
+def all_body_errors(eng, r, m, G, rows, device):
+    """Per-body relative acceleration error of the engine's mode on the FP64 state, over
+    every body, against the GPU's FP64 mode (Engine 'fp64', FP64 all pairs); the FP64
+    mode is checked against the CPU FP64 oracle on `rows` in the same call."""
     import oracle
-    a = eng.forces().cpu().numpy()[rows]
-    r32 = r.astype(np.float32).astype(np.float64)
-    gm32 = (G * m).astype(np.float32).astype(np.float64)
-    e_arith = oracle.rel_err_per_body(a, oracle.accel_fp64(r32, gm32, 1.0, rows=rows,
-                                                           coincident=True)).max()
-    e_state = oracle.rel_err_per_body(a, oracle.accel_fp64(r, G * m, 1.0, rows=rows,
-                                                           coincident=True)).max()
-    return float(e_arith), float(e_state)
+    from gravitation_gb300.engine import Engine
+    n = len(m)
+    a = eng.forces().cpu().numpy()
+    e64 = Engine([n], 1.0, mode='fp64', device=device)
+    e64.set_state(r, np.zeros_like(r), G * m)
+    a64 = e64.forces().cpu().numpy()
+    e64.raise_on_device_error()
+    del e64
+    ref_rows = oracle.accel_fp64(r, G * m, 1.0, rows=rows, coincident=True)
+    pin = float(oracle.rel_err_per_body(a64[rows], ref_rows).max())
+    err = oracle.rel_err_per_body(a, a64)
+    return {'max_rel_err_all_bodies_fp64_state': float(err.max()),
+            'p999_rel_err': float(np.quantile(err, 0.999)),
+            'median_rel_err': float(np.median(err)),
+            'bodies_above_1e-5': int((err > 1e-5).sum()),
+            'bodies': int(n),
+            'reference': 'GPU FP64 mode on the same FP64 state (every body)',
+            'fp64_mode_vs_cpu_oracle_max_rel_err': pin,
+            'fp64_mode_bodies_checked_against_oracle': int(len(rows)),
+            'max_rel_err_sampled_vs_cpu_oracle': float(
+                oracle.rel_err_per_body(a[rows], ref_rows).max())}
 
 
 def run_ours(args):
@@ -376,11 +397,11 @@ def run_ours(args):
         return 0
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=device)
 
-    # accuracy on sampled bodies before timing (FP64 oracle on the host)
+    # accuracy of every body before timing (GPU FP64 mode; it against the CPU oracle)
     rows = np.random.default_rng(17).choice(n, 64, replace=False)
-    e_arith, e_state = (None, None)
+    accuracy = None
     if rank == 0:
-        e_arith, e_state = sampled_errors(eng, r, m, G_DEFAULT, rows)
+        accuracy = all_body_errors(eng, r, m, G_DEFAULT, rows, local)
         eng.set_state(r, v, gm)
 
     for _ in range(args.warmup):
@@ -457,8 +478,9 @@ def run_ours(args):
         'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': max_ms,
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
         'dtype': 'f32',
-        'dtype_detail': ('FP32 pair terms into compensated FP32 (hi, lo) sums; FP64 state and '
-                         'stage 2'),
+        'dtype_detail': ('FP32 pair terms into compensated FP32 (hi, lo) sums%s; FP64 state and '
+                         'stage 2' % (', near pairs from double-single separations'
+                                      if args.mode in ('fp32n', 'fp32un') else '')),
         'data': 'synthetic (seeded uniform cube; the reference ships no dataset)',
         'config': {'workload': workload_name(n, args.mode),
                    'n': n, 'mode': args.mode,
@@ -474,9 +496,7 @@ def run_ours(args):
                      'peak_kind': 'measured live (grav_fp32_peak_probe FFMA kernel)',
                      'peak_formula_tflops_at_max_clock':
                          info.sm_count * 128 * 2 * (clk.get('sm_max_mhz') or 2070) * 1e6 / 1e12},
-        'accuracy': {'max_rel_err_vs_fp64_oracle_on_fp32_positions': e_arith,
-                     'max_rel_err_vs_fp64_oracle_on_fp64_state': e_state,
-                     'bodies_sampled': int(len(rows))},
+        'accuracy': accuracy,
         'clocks': clk,
         'gpu_launches': 2 * args.steps,
         'e2e': e2e,

@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, 'libgravgb300.so')
 
 # ---- constants (mirror of the header) -------------------------------------------
-GRAV_ABI_VERSION = 3
+GRAV_ABI_VERSION = 4
 GRAV_OK = 0
 GRAV_E_ARG = -1
 GRAV_E_TILE = -2
@@ -30,9 +30,13 @@ GRAV_S2_WRITE_A = 2
 GRAV_S2_PREPARE = 4
 
 GRAV_MODE_FP32CU = 4
+GRAV_MODE_FP32N = 5
+GRAV_MODE_FP32UN = 6
+GRAV_NEAR_KAPPA = 20
 MODES = {'fp32': GRAV_MODE_FP32, 'fp32c': GRAV_MODE_FP32C, 'fp64': GRAV_MODE_FP64,
-         'fp32u': GRAV_MODE_FP32U, 'fp32cu': GRAV_MODE_FP32CU}
-PAIR_MODES = ('fp32u', 'fp32cu', GRAV_MODE_FP32U, GRAV_MODE_FP32CU)
+         'fp32u': GRAV_MODE_FP32U, 'fp32cu': GRAV_MODE_FP32CU, 'fp32n': GRAV_MODE_FP32N,
+         'fp32un': GRAV_MODE_FP32UN}
+PAIR_MODES = ('fp32u', 'fp32cu', 'fp32un', GRAV_MODE_FP32U, GRAV_MODE_FP32CU, GRAV_MODE_FP32UN)
 
 
 class GravError(RuntimeError):

@@ -8,14 +8,13 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
+#include <set>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "grav_types.h"
-
-namespace grav {
-cudaError_t launch_stage2(const grav_batch& b, int flags, cudaStream_t stream);
-}
 
 namespace {
 
@@ -45,7 +44,8 @@ int cuda_fail(cudaError_t e, const char* what)
 int stage1_table_for(int mode, const grav::Stage1Kernel** tab)
 {
 	if (mode == GRAV_MODE_FP64) return grav::stage1_table_f64(tab);
-	if (mode == GRAV_MODE_FP32U || mode == GRAV_MODE_FP32CU) return grav::stage1_table_sym(tab);
+	if (mode == GRAV_MODE_FP32U || mode == GRAV_MODE_FP32CU || mode == GRAV_MODE_FP32UN)
+		return grav::stage1_table_sym(tab);
 	return grav::stage1_table_f32(tab);
 }
 
@@ -60,10 +60,28 @@ const grav::Stage1Kernel* find_kernel(int mode, int bpt, int threads, int jtile)
 	return nullptr;
 }
 
+// Raise a kernel's dynamic shared-memory limit to what its launch asks for, once per
+// kernel and device: static plus dynamic shared memory above 48 KB (the near-pair
+// kernels' row buffers) needs the opt-in.  Called before occupancy queries and launches.
+cudaError_t ensure_smem(const grav::Stage1Kernel* k)
+{
+	static std::mutex mu;
+	static std::set<std::pair<int, const void*>> done;
+	int dev = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if (e != cudaSuccess) return e;
+	std::lock_guard<std::mutex> lock(mu);
+	if (done.count({dev, k->fn})) return cudaSuccess;
+	e = cudaFuncSetAttribute(k->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, k->smem_bytes);
+	if (e == cudaSuccess) done.insert({dev, k->fn});
+	return e;
+}
+
 bool valid_mode(int mode)
 {
 	return mode == GRAV_MODE_FP32 || mode == GRAV_MODE_FP32C || mode == GRAV_MODE_FP64 ||
-		mode == GRAV_MODE_FP32U || mode == GRAV_MODE_FP32CU;
+		mode == GRAV_MODE_FP32U || mode == GRAV_MODE_FP32CU || mode == GRAV_MODE_FP32N ||
+		mode == GRAV_MODE_FP32UN;
 }
 
 int check_batch(const grav_batch* b)
@@ -152,9 +170,10 @@ int grav_occupancy(int mode, const grav_tile* tile, int32_t* ctas_per_sm)
 	if (!k)
 		return fail(GRAV_E_TILE, "tile bpt=%d threads=%d jtile=%d not compiled for mode %d",
 			tile->bpt, tile->threads, tile->jtile, mode);
+	cudaError_t e = ensure_smem(k);
+	if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute (dynamic shared memory)");
 	int blocks = 0;
-	cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k->fn, k->threads,
-		k->smem_bytes);
+	e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k->fn, k->threads, k->smem_bytes);
 	if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
 	*ctas_per_sm = blocks;
 	return ok();
@@ -319,7 +338,9 @@ int64_t grav_pos_bytes(int mode, int64_t n_pad_total)
 {
 	if (!valid_mode(mode) || n_pad_total < 0) return fail(GRAV_E_ARG, "bad mode or size");
 	if (mode == GRAV_MODE_FP64) return n_pad_total * 32;
-	if (mode == GRAV_MODE_FP32C || mode == GRAV_MODE_FP32CU) return n_pad_total * 32;
+	if (mode == GRAV_MODE_FP32C || mode == GRAV_MODE_FP32CU || mode == GRAV_MODE_FP32N ||
+		mode == GRAV_MODE_FP32UN)
+		return n_pad_total * 32;
 	return n_pad_total * 16;
 }
 
@@ -361,10 +382,12 @@ int grav_stage1(const grav_batch* b, void* stream)
 	if (!k)
 		return fail(GRAV_E_TILE, "tile bpt=%d threads=%d jtile=%d not compiled for mode %d",
 			b->tile.bpt, b->tile.threads, b->tile.jtile, b->mode);
+	cudaError_t e = ensure_smem(k);
+	if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute (dynamic shared memory)");
 	grav_batch copy = *b;
 	void* args[] = {&copy};
 	cudaStream_t st = static_cast<cudaStream_t>(stream);
-	cudaError_t e = k->dependent
+	e = k->dependent
 		? grav::launch_dependent(k->fn, b->tile.grid, b->tile.threads, k->smem_bytes, st, args)
 		: cudaLaunchKernel(k->fn, dim3(b->tile.grid), dim3(b->tile.threads), args, k->smem_bytes, st);
 	if (e != cudaSuccess) return cuda_fail(e, "stage-1 kernel launch");

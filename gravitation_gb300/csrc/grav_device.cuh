@@ -125,6 +125,65 @@ __device__ __forceinline__ void grid_dep_launch()
 	asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+// Near-pair correction (GRAV_MODE_FP32N / GRAV_MODE_FP32UN).  Rounding a coordinate x
+// to FP32 moves it by up to 2^-24 |x|, so the FP32 separation of two bodies far from the
+// origin but close to each other carries a relative error of order 2^-24 |x| / |d|.
+// The near modes evaluate every pair with r2 < near_threshold() (|d| below
+// max|x| / GRAV_NEAR_KAPPA, max|x| over the coordinates of the thread's rows) a second
+// time from the double-single separation d_a = (hi_j - hi_i) + (lo_j - lo_i) and add the
+// difference.  Beyond that distance the FP32 separation is within
+// 2^-24 (sqrt(3) (2 kappa + 1) + 1) of the exact one (~4.5e-6 relative pair-force error
+// at kappa = 20, a bound; measured body errors stay below 1e-6).
+__device__ __forceinline__ float near_scale(float x, float y, float z)
+{
+	return fmaxf(fabsf(x), fmaxf(fabsf(y), fabsf(z)));
+}
+
+__device__ __forceinline__ float near_threshold(float max_abs_coord)
+{
+	constexpr float inv_k2 = 1.0f / (GRAV_NEAR_KAPPA * GRAV_NEAR_KAPPA);
+	return max_abs_coord * max_abs_coord * inv_k2;
+}
+
+// Running minimum of the r2 values of a thread's B rows for the near test, one
+// three-input min per two rows (min.f32 with three operands, sm_100 and later): call
+// with k = 0 .. B-1 in order; `prev` holds the previous row's r2 between calls.
+__device__ __forceinline__ float min3f(float a, float b, float c)
+{
+	float r;
+	asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+	return r;
+}
+
+template <int B>
+__device__ __forceinline__ void near_min_step(int k, float r2, float& m, float& prev)
+{
+	if (k == 0) m = r2;
+	else if ((k & 1) == 0) m = min3f(m, prev, r2);
+	else if (k == B - 1) m = fminf(m, r2);
+	prev = r2;
+}
+
+// (ex, ey, ez) = d_a |d_a|^-3 - d |d|^-3 for the pair whose FP32 separation is (dx, dy,
+// dz) with r2 = |d|^2 + eps2 (as the main loop formed it), lj / li the low parts of the
+// column and row bodies; zero unless `on`.  The caller adds Gm_j e to the row's sum and
+// -Gm_i e to the column's, which replaces the FP32 pair term by the double-single one.
+__device__ __forceinline__ void near_delta(float dx, float dy, float dz, float r2,
+	const float4& lj, const float4& li, float eps2, bool on, float& ex, float& ey, float& ez)
+{
+	const float ax = dx + (lj.x - li.x);
+	const float ay = dy + (lj.y - li.y);
+	const float az = dz + (lj.z - li.z);
+	const float ra2 = fmaf(az, az, fmaf(ay, ay, fmaf(ax, ax, eps2)));
+	const float ia = rsqrt_sfu(ra2);
+	const float ia3 = ia * (ia * ia);
+	const float i1 = rsqrt_sfu(r2);
+	const float i3 = i1 * (i1 * i1);
+	ex = on ? fmaf(ax, ia3, -(dx * i3)) : 0.f;
+	ey = on ? fmaf(ay, ia3, -(dy * i3)) : 0.f;
+	ez = on ? fmaf(az, ia3, -(dz * i3)) : 0.f;
+}
+
 // Combine the compensated FP32 sums (H, L) of the WIDTH lanes of an aligned lane group
 // by an xor butterfly: H by TwoSum, L and the rounding error added.  Every lane ends
 // with the same bits: TwoSum's error term is the exact rounding error of H_a + H_b in

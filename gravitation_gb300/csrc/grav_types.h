@@ -18,6 +18,12 @@ struct Stage1Kernel {
 	bool dependent;       // waits with grid_dep_wait(): may launch as a programmatic dependent
 };
 
+// Stage-2 kernel (stage2.cu).  dependent = true launches it with programmatic stream
+// serialization (it reads only plan tables before its grid_dep_wait()); false launches
+// it the ordinary way, for callers whose previous kernel wrote those tables.
+cudaError_t launch_stage2(const grav_batch& b, int flags, cudaStream_t stream,
+	bool dependent = true);
+
 // Kernel tables, one per translation unit (stage1_f32.cu, stage1_f64.cu).
 int stage1_table_f32(const Stage1Kernel** out);
 int stage1_table_f64(const Stage1Kernel** out);

@@ -6,8 +6,8 @@
 // captured or timed, or embedded hosts that reserve all device memory up front.
 // grav_forces_noalloc serves them: the caller passes only the inputs (positions and
 // G*m) and the output (accelerations); every piece of scratch memory the stage-1 and
-// stage-2 kernels need -- plan tables, padded FP32 positions, FP64 partial sums and
-// the device error flag -- lives in the file-scope array below, sized for at most
+// stage-2 kernels need -- plan tables, padded FP32 positions, FP32 (hi, lo) partial
+// sums and the device error flag -- lives in the file-scope array below, sized for at most
 // GRAV_NOALLOC_MAX_N bodies (about 3.8 MB, held by every GPU that loads the library
 // until the process exits).
 //
@@ -17,8 +17,10 @@
 // cudaGetSymbolAddress and keeps it; that first call should come before any stream
 // capture.  All calls share the array and it keeps the last call's contents: each
 // call rebuilds the plan tables, rewrites all the padded positions and partial slots it
-// reads and zeroes the error flag, so nothing stale is read, but two calls whose work
-// overlaps on the GPU (different streams, no ordering between them) race on it.
+// reads and zeroes the internal error flag, so nothing stale is read, but two calls whose
+// work overlaps on the GPU (different streams, no ordering between them) race on it.
+// A caller-supplied error flag is never cleared here (the caller owns it and may share
+// it); with none, device-side timeouts land in the internal flag and go unreported.
 #include <cstdio>
 #include <mutex>
 
@@ -29,7 +31,6 @@ namespace grav {
 int record_error(int code, const char* msg);
 }
 
-extern "C" int grav_prepare(const grav_batch* b, void* stream);
 extern "C" int grav_stage1(const grav_batch* b, void* stream);
 extern "C" int grav_stage2(const grav_batch* b, int flags, void* stream);
 
@@ -105,8 +106,10 @@ __host__ __device__ int plan_single(int n, int grid, long long units, grav_seg_d
 	return slots;
 }
 
-__global__ void noalloc_plan_kernel(unsigned char* scratch, int n, int grid, long long units,
-	int32_t* err)
+// Writes the plan tables and clears the internal error flag (a caller's flag is left
+// alone).  The launches after it read the tables, so the next one (the prepare pass) is
+// launched the ordinary way: it starts only after this kernel has completed.
+__global__ void noalloc_plan_kernel(unsigned char* scratch, int n, int grid, long long units)
 {
 	if (blockIdx.x != 0 || threadIdx.x != 0) return;
 	grav_univ_desc* u = reinterpret_cast<grav_univ_desc*>(scratch + OFF_UNIV);
@@ -116,7 +119,7 @@ __global__ void noalloc_plan_kernel(unsigned char* scratch, int n, int grid, lon
 	u->n_jtiles = (n + NA_JTILE - 1) / NA_JTILE;
 	u->T = 0.0;
 	plan_single(n, grid, units, reinterpret_cast<grav_seg_desc*>(scratch + OFF_SEG));
-	*err = GRAV_DEV_OK;
+	*reinterpret_cast<int32_t*>(scratch + OFF_ERR) = GRAV_DEV_OK;
 }
 
 int device_setup(DeviceSetup** out)
@@ -182,7 +185,7 @@ extern "C" int grav_forces_noalloc(const double* r, double* a, int32_t n, double
 	const int n_slots = plan_single(n, grid, units, nullptr);
 	int32_t* errp = err ? err : reinterpret_cast<int32_t*>(s->scratch + OFF_ERR);
 
-	noalloc_plan_kernel<<<1, 32, 0, st>>>(s->scratch, n, grid, units, errp);
+	noalloc_plan_kernel<<<1, 32, 0, st>>>(s->scratch, n, grid, units);
 	cudaError_t e = cudaGetLastError();
 	if (e != cudaSuccess) return na_fail(GRAV_E_CUDA, "plan kernel launch failed (%lld)", (long long)e);
 
@@ -204,7 +207,11 @@ extern "C" int grav_forces_noalloc(const double* r, double* a, int32_t n, double
 	b.part = reinterpret_cast<double*>(s->scratch + OFF_PART);
 	b.a_out = a;
 	b.err = errp;
-	if ((rc = grav_prepare(&b, st)) != GRAV_OK) return rc;
+	// the prepare pass reads the tables the plan kernel just wrote before its
+	// grid_dep_wait(), so it must not start early: an ordinary launch
+	e = grav::launch_stage2(b, GRAV_S2_PREPARE, st, false);
+	if (e != cudaSuccess)
+		return na_fail(GRAV_E_CUDA, "prepare kernel launch failed (%lld)", (long long)e);
 	if ((rc = grav_stage1(&b, st)) != GRAV_OK) return rc;
 	return grav_stage2(&b, GRAV_S2_WRITE_A, st);
 }

@@ -23,6 +23,11 @@
 // GRAV_MODE_FP32C reads a second FP32 array with the low parts of the positions
 // (x = hi + lo) and forms d = (hi_j - hi_i) + (lo_j - lo_i): the separation is then
 // accurate to FP32 relative precision however far the bodies are from the origin.
+// GRAV_MODE_FP32N keeps the FP32 loop and compares each pair's r2 with the near radius
+// (grav_device.cuh, near_threshold); a step where any lane of the warp met a nearer
+// pair re-evaluates those pairs from the double-single separation (near_delta).  The
+// j-tiles that hold the CTA's own rows also require r2 > eps2, so that the self pairs
+// (d = 0) do not send every warp down that cold path.
 #include "grav_device.cuh"
 
 namespace grav {
@@ -30,11 +35,15 @@ namespace grav {
 template <int MODE, int B, int T, int J>
 __global__ void __launch_bounds__(T) stage1_f32_kernel(const grav_batch b)
 {
-	constexpr int NP = (MODE == GRAV_MODE_FP32C) ? 2 : 1;  // float4 arrays per body
+	constexpr bool DS = MODE == GRAV_MODE_FP32C;            // double-single separations
+	constexpr bool NEAR = MODE == GRAV_MODE_FP32N;          // ... for near pairs only
+	constexpr int NP = (DS || NEAR) ? 2 : 1;                // float4 arrays per body
 	constexpr int IT = B * T;                               // i-tile
 	constexpr uint32_t TILE_BYTES = J * sizeof(float4);
 	extern __shared__ __align__(128) float4 smem_tiles[];   // [2 buffers][NP][J]
 	__shared__ __align__(8) uint64_t bar[2];
+	// low parts of this thread's rows (NEAR), read back only by the thread that wrote them
+	__shared__ float4 rowlo[NEAR ? B : 1][NEAR ? T : 1];
 
 	const int tid = threadIdx.x;
 	const int64_t U = b.n_units;
@@ -91,13 +100,14 @@ __global__ void __launch_bounds__(T) stage1_f32_kernel(const grav_batch b)
 		float xl[B], yl[B], zl[B];
 		float fx[B], fy[B], fz[B];
 		float hx[B], hy[B], hz[B], lx[B], ly[B], lz[B];  // compensated per-body sums
+		float xmax = 0.f;                                // NEAR: largest |coordinate| of the rows
 #pragma unroll
 		for (int k = 0; k < B; ++k) {
 			const float4 p = pos[ibase + tid + k * T];
 			xi[k] = p.x;
 			yi[k] = p.y;
 			zi[k] = p.z;
-			if (NP == 2) {
+			if (DS) {
 				const float4 q = poslo[ibase + tid + k * T];
 				xl[k] = q.x;
 				yl[k] = q.y;
@@ -105,9 +115,14 @@ __global__ void __launch_bounds__(T) stage1_f32_kernel(const grav_batch b)
 			} else {
 				xl[k] = yl[k] = zl[k] = 0.f;
 			}
+			if (NEAR) {
+				rowlo[NEAR ? k : 0][NEAR ? tid : 0] = poslo[ibase + tid + k * T];
+				xmax = fmaxf(xmax, near_scale(p.x, p.y, p.z));
+			}
 			fx[k] = fy[k] = fz[k] = 0.f;
 			hx[k] = hy[k] = hz[k] = lx[k] = ly[k] = lz[k] = 0.f;
 		}
+		const float thr = near_threshold(xmax);
 
 		for (int t = 0; t < nt; ++t, ++gt) {
 			const int bs = gt & 1;
@@ -126,22 +141,27 @@ __global__ void __launch_bounds__(T) stage1_f32_kernel(const grav_batch b)
 			}
 			const float4* __restrict__ sj = smem_tiles + (bs * NP) * J;
 			const float4* __restrict__ sl = sj + J;
+			// NEAR: does this j-tile hold rows of this CTA (their self pairs)?
+			const int64_t jl0 = (jt0 + t) * J;
+			const bool own = jl0 < S.il0 + IT && jl0 + J > S.il0;
 #pragma unroll 4
 			for (int j = 0; j < J; ++j) {
 				const float4 pj = sj[j];
 				float4 lj = make_float4(0.f, 0.f, 0.f, 0.f);
-				if (NP == 2) lj = sl[j];
+				if (DS) lj = sl[j];
+				bool near = false;
 #pragma unroll
 				for (int k = 0; k < B; ++k) {
 					float dx = pj.x - xi[k];
 					float dy = pj.y - yi[k];
 					float dz = pj.z - zi[k];
-					if (NP == 2) {
+					if (DS) {
 						dx = dx + (lj.x - xl[k]);
 						dy = dy + (lj.y - yl[k]);
 						dz = dz + (lj.z - zl[k]);
 					}
 					const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+					if (NEAR) near |= own ? (r2 < thr) & (r2 > eps2) : (r2 < thr);
 					const float inv = rsqrt_sfu(r2);
 					const float inv2 = inv * inv;
 					float w = pj.w * inv;
@@ -149,6 +169,25 @@ __global__ void __launch_bounds__(T) stage1_f32_kernel(const grav_batch b)
 					fx[k] = fmaf(dx, w, fx[k]);
 					fy[k] = fmaf(dy, w, fy[k]);
 					fz[k] = fmaf(dz, w, fz[k]);
+				}
+				if (NEAR && __any_sync(0xffffffffu, near)) {
+					// cold path: this step's pairs within the near radius again, from the
+					// double-single separation
+					lj = sl[j];
+#pragma unroll
+					for (int k = 0; k < B; ++k) {
+						const float dx = pj.x - xi[k], dy = pj.y - yi[k], dz = pj.z - zi[k];
+						const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+						const bool nk = (r2 < thr) & (r2 > eps2);
+						if (__any_sync(0xffffffffu, nk)) {
+							float ex, ey, ez;
+							near_delta(dx, dy, dz, r2, lj, rowlo[NEAR ? k : 0][NEAR ? tid : 0],
+								eps2, nk, ex, ey, ez);
+							fx[k] = fmaf(ex, pj.w, fx[k]);
+							fy[k] = fmaf(ey, pj.w, fy[k]);
+							fz[k] = fmaf(ez, pj.w, fz[k]);
+						}
+					}
 				}
 			}
 #pragma unroll
@@ -189,7 +228,7 @@ __global__ void __launch_bounds__(T) stage1_f32_kernel(const grav_batch b)
 
 #define GRAV_F32_ENTRY(MODE, B, T, J) \
 	{MODE, B, T, J, reinterpret_cast<const void*>(&stage1_f32_kernel<MODE, B, T, J>), \
-		2 * ((MODE == GRAV_MODE_FP32C) ? 2 : 1) * J * 16, true}
+		2 * ((MODE == GRAV_MODE_FP32) ? 1 : 2) * J * 16, true}
 
 static const Stage1Kernel k_table_f32[] = {
 	GRAV_F32_ENTRY(GRAV_MODE_FP32, 1, 128, 128),
@@ -204,6 +243,12 @@ static const Stage1Kernel k_table_f32[] = {
 	GRAV_F32_ENTRY(GRAV_MODE_FP32C, 2, 128, 128),
 	GRAV_F32_ENTRY(GRAV_MODE_FP32C, 4, 128, 256),
 	GRAV_F32_ENTRY(GRAV_MODE_FP32C, 4, 256, 256),
+	GRAV_F32_ENTRY(GRAV_MODE_FP32N, 1, 128, 128),
+	GRAV_F32_ENTRY(GRAV_MODE_FP32N, 2, 128, 128),
+	GRAV_F32_ENTRY(GRAV_MODE_FP32N, 4, 128, 128),
+	GRAV_F32_ENTRY(GRAV_MODE_FP32N, 4, 128, 256),
+	GRAV_F32_ENTRY(GRAV_MODE_FP32N, 8, 128, 256),
+	GRAV_F32_ENTRY(GRAV_MODE_FP32N, 4, 256, 256),
 };
 
 int stage1_table_f32(const Stage1Kernel** out)

@@ -1,4 +1,5 @@
-// stage1_sym.cu -- stage 1 over unique pairs (GRAV_MODE_FP32U).
+// stage1_sym.cu -- stage 1 over unique pairs (GRAV_MODE_FP32U, GRAV_MODE_FP32CU,
+// GRAV_MODE_FP32UN).
 //
 // The reference's CPU kernels visit every unordered pair once and update both bodies
 // (np1.py:81-95, _lib1_/lib.c:78-114, _lib4_/lib.c:244-317: a_i -= ..., a_j += ...).
@@ -28,10 +29,20 @@
 
 namespace grav {
 
-// NP = 1: FP32 positions (GRAV_MODE_FP32U).  NP = 2: FP32 hi and lo parts of the FP64
-// positions (GRAV_MODE_FP32CU): d = (hi_j - hi_i) + (lo_j - lo_i), exact to FP32
-// relative precision however far from the origin the bodies are (+6 FADD per pair).
-template <int B, int W, int JT, int UNROLL = 4, int NP = 1>
+// KIND selects the separations:
+//   SYM_PLAIN (GRAV_MODE_FP32U): FP32 positions, d = hi_j - hi_i.
+//   SYM_DS    (GRAV_MODE_FP32CU): FP32 hi and lo parts of the FP64 positions,
+//             d = (hi_j - hi_i) + (lo_j - lo_i), exact to FP32 relative precision however
+//             far from the origin the bodies are (+6 FADD per pair).
+//   SYM_NEAR  (GRAV_MODE_FP32UN): the SYM_PLAIN loop plus one compare per pair against
+//             the near radius (grav_device.cuh, near_threshold); a step of the loop where
+//             any lane of the warp met a near pair re-evaluates those pairs from the
+//             double-single separation and adds the difference (near_delta).  Near pairs
+//             are rare (~3e-5 of the pairs of the N = 65536 uniform cube), so this path is
+//             cold; it is warp-uniform, so it costs no divergence.
+enum { SYM_PLAIN = 0, SYM_DS = 1, SYM_NEAR = 2 };
+
+template <int B, int W, int JT, int UNROLL = 4, int KIND = SYM_PLAIN>
 __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 {
 	constexpr int T = 32 * W;
@@ -39,14 +50,24 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 	constexpr int TPB = R / JT;         // j-tiles per block
 	constexpr int NCH = JT / 32;        // 32-body chunks per j-tile
 	constexpr uint32_t TILE_BYTES = JT * sizeof(float4);
+	constexpr int NP = KIND == SYM_PLAIN ? 1 : 2;   // position arrays copied per j-tile
+	constexpr bool DS = KIND == SYM_DS;             // double-single separations everywhere
+	constexpr bool NEAR = KIND == SYM_NEAR;         // double-single for near pairs only
 	static_assert(R % JT == 0 && JT % 32 == 0, "tile shapes");
-	static_assert(NP == 1 || NP == 2, "one or two position arrays");
 	extern __shared__ __align__(128) float4 sym_tiles[];   // [2 buffers][NP][JT]
 	// column sums of a j-tile, one row per warp: every warp writes each chunk of the tile
 	// once, and the flush adds the warps in a fixed order (no shared-memory atomics, whose
 	// order would depend on warp timing)
 	__shared__ float colacc[W][3][JT];
 	__shared__ __align__(8) uint64_t bar[2];
+	// low parts of this thread's rows (NEAR): read only on the cold correction path, by
+	// the thread that wrote them ([k][tid]: conflict-free 16-byte accesses)
+	__shared__ float4 rowlo[NEAR ? B : 1][NEAR ? T : 1];
+	// NEAR with 8 rows per thread keeps the compensated row sums (hi, lo) in shared memory
+	// instead of 48 registers, touched once per j-tile: the cold correction path's
+	// registers would otherwise cost a resident CTA per SM
+	constexpr bool SS = NEAR && B >= 8;
+	__shared__ float2 csum[SS ? 3 : 1][SS ? B : 1][SS ? T : 1];
 
 	const int tid = threadIdx.x;
 	const int lane = tid & 31;
@@ -112,8 +133,9 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 		// rows of this warp: w*32*B + k*32 + lane
 		const int64_t ibase = Uu.pad_off + S.il0 + warp * 32 * B + lane;
 		float xi[B], yi[B], zi[B], gi[B], fx[B], fy[B], fz[B];
-		float xl[B], yl[B], zl[B];                       // low parts (NP == 2)
+		float xl[B], yl[B], zl[B];                       // low parts (DS)
 		float hx[B], hy[B], hz[B], lx[B], ly[B], lz[B];  // compensated row sums
+		float xmax = 0.f;                                // NEAR: largest |coordinate| of the rows
 #pragma unroll
 		for (int k = 0; k < B; ++k) {
 			const float4 p = pos[ibase + k * 32];
@@ -121,7 +143,7 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 			yi[k] = p.y;
 			zi[k] = p.z;
 			gi[k] = p.w;
-			if (NP == 2) {
+			if (DS) {
 				const float4 q = pos[b.n_pad_total + ibase + k * 32];
 				xl[k] = q.x;
 				yl[k] = q.y;
@@ -129,9 +151,18 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 			} else {
 				xl[k] = yl[k] = zl[k] = 0.f;
 			}
+			if (NEAR) {
+				rowlo[NEAR ? k : 0][NEAR ? tid : 0] = pos[b.n_pad_total + ibase + k * 32];
+				xmax = fmaxf(xmax, near_scale(p.x, p.y, p.z));
+			}
 			fx[k] = fy[k] = fz[k] = 0.f;
 			hx[k] = hy[k] = hz[k] = lx[k] = ly[k] = lz[k] = 0.f;
+			if (SS) {
+#pragma unroll
+				for (int cpt = 0; cpt < 3; ++cpt) csum[SS ? cpt : 0][SS ? k : 0][SS ? tid : 0] = make_float2(0.f, 0.f);
+			}
 		}
+		const float thr = near_threshold(xmax);
 
 		for (int t = 0; t < nt; ++t, ++gt) {
 			const int bs = gt & 1;
@@ -153,27 +184,51 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 			const float4* __restrict__ sjl = sj + JT;  // low parts (NP == 2)
 			const int blkJ = static_cast<int>(jt / TPB);
 			if (blkJ == blkI) {
-				// diagonal block: every ordered pair of the block once, rows only
+				// diagonal block: every ordered pair of the block once, rows only.  In NEAR
+				// mode a tile that holds this warp's own rows meets their self pairs (d = 0,
+				// r2 = eps2): there the near test also requires r2 > eps2, so that self pairs
+				// do not send the warp down the correction path
+				const int jl0 = static_cast<int>(jt - static_cast<int64_t>(blkI) * TPB) * JT;
+				const bool own = jl0 < (warp + 1) * 32 * B && jl0 + JT > warp * 32 * B;
 #pragma unroll 4
 				for (int j = 0; j < JT; ++j) {
 					const float4 pj = sj[j];
 					float4 lj = make_float4(0.f, 0.f, 0.f, 0.f);
-					if (NP == 2) lj = sjl[j];
+					if (DS) lj = sjl[j];
+					bool near = false;
 #pragma unroll
 					for (int k = 0; k < B; ++k) {
 						float dx = pj.x - xi[k], dy = pj.y - yi[k], dz = pj.z - zi[k];
-						if (NP == 2) {
+						if (DS) {
 							dx = dx + (lj.x - xl[k]);
 							dy = dy + (lj.y - yl[k]);
 							dz = dz + (lj.z - zl[k]);
 						}
 						const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+						if (NEAR) near |= own ? (r2 < thr) & (r2 > eps2) : (r2 < thr);
 						const float inv = rsqrt_sfu(r2);
 						float w = pj.w * inv;
 						w = w * (inv * inv);
 						fx[k] = fmaf(dx, w, fx[k]);
 						fy[k] = fmaf(dy, w, fy[k]);
 						fz[k] = fmaf(dz, w, fz[k]);
+					}
+					if (NEAR && __any_sync(0xffffffffu, near)) {
+						lj = sjl[j];
+#pragma unroll
+						for (int k = 0; k < B; ++k) {
+							const float dx = pj.x - xi[k], dy = pj.y - yi[k], dz = pj.z - zi[k];
+							const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+							const bool nk = (r2 < thr) & (r2 > eps2);
+							if (__any_sync(0xffffffffu, nk)) {
+								float ex, ey, ez;
+								near_delta(dx, dy, dz, r2, lj, rowlo[NEAR ? k : 0][NEAR ? tid : 0],
+									eps2, nk, ex, ey, ez);
+								fx[k] = fmaf(ex, pj.w, fx[k]);
+								fy[k] = fmaf(ey, pj.w, fy[k]);
+								fz[k] = fmaf(ez, pj.w, fz[k]);
+							}
+						}
 					}
 				}
 			} else {
@@ -188,16 +243,18 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 					for (int st = 0; st < 32; ++st) {
 						const float4 pj = sc[(lane + st) & 31];
 						float4 lj = make_float4(0.f, 0.f, 0.f, 0.f);
-						if (NP == 2) lj = scl[(lane + st) & 31];
+						if (DS) lj = scl[(lane + st) & 31];
+						float rmin = 0.f, rprev = 0.f;   // NEAR: smallest r2 of this step
 #pragma unroll
 						for (int k = 0; k < B; ++k) {
 							float dx = pj.x - xi[k], dy = pj.y - yi[k], dz = pj.z - zi[k];
-							if (NP == 2) {
+							if (DS) {
 								dx = dx + (lj.x - xl[k]);
 								dy = dy + (lj.y - yl[k]);
 								dz = dz + (lj.z - zl[k]);
 							}
 							const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+							if (NEAR) near_min_step<B>(k, r2, rmin, rprev);
 							const float inv = rsqrt_sfu(r2);
 							const float inv3 = inv * (inv * inv);
 							const float wj = pj.w * inv3;
@@ -208,6 +265,28 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 							cx = fmaf(-dx, wi, cx);
 							cy = fmaf(-dy, wi, cy);
 							cz = fmaf(-dz, wi, cz);
+						}
+						if (NEAR && __any_sync(0xffffffffu, rmin < thr)) {
+							// cold path: the pairs of this step closer than the near radius
+							// again, from the double-single separation (row and column)
+							lj = scl[(lane + st) & 31];
+#pragma unroll
+							for (int k = 0; k < B; ++k) {
+								const float dx = pj.x - xi[k], dy = pj.y - yi[k], dz = pj.z - zi[k];
+								const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+								const bool nk = (r2 < thr) & (r2 > eps2);
+								if (__any_sync(0xffffffffu, nk)) {
+									float ex, ey, ez;
+									near_delta(dx, dy, dz, r2, lj,
+										rowlo[NEAR ? k : 0][NEAR ? tid : 0], eps2, nk, ex, ey, ez);
+									fx[k] = fmaf(ex, pj.w, fx[k]);
+									fy[k] = fmaf(ey, pj.w, fy[k]);
+									fz[k] = fmaf(ez, pj.w, fz[k]);
+									cx = fmaf(-ex, gi[k], cx);
+									cy = fmaf(-ey, gi[k], cy);
+									cz = fmaf(-ez, gi[k], cz);
+								}
+							}
 						}
 						const int src = (lane + 1) & 31;
 						cx = __shfl_sync(0xffffffffu, cx, src);
@@ -242,9 +321,21 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 			}
 #pragma unroll
 			for (int k = 0; k < B; ++k) {
-				two_sum_acc(hx[k], lx[k], fx[k]);
-				two_sum_acc(hy[k], ly[k], fy[k]);
-				two_sum_acc(hz[k], lz[k], fz[k]);
+				if (SS) {
+					float2* cs = &csum[0][SS ? k : 0][SS ? tid : 0];
+					constexpr int CS = SS ? B * T : 0;   // stride between components
+					float2 h0 = cs[0], h1 = cs[CS], h2 = cs[2 * CS];
+					two_sum_acc(h0.x, h0.y, fx[k]);
+					two_sum_acc(h1.x, h1.y, fy[k]);
+					two_sum_acc(h2.x, h2.y, fz[k]);
+					cs[0] = h0;
+					cs[CS] = h1;
+					cs[2 * CS] = h2;
+				} else {
+					two_sum_acc(hx[k], lx[k], fx[k]);
+					two_sum_acc(hy[k], ly[k], fy[k]);
+					two_sum_acc(hz[k], lz[k], fz[k]);
+				}
 				fx[k] = fy[k] = fz[k] = 0.f;
 			}
 		}
@@ -256,9 +347,15 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 		const int r0 = warp * 32 * B + lane;
 #pragma unroll
 		for (int k = 0; k < B; ++k) {
-			out[r0 + k * 32] = make_float2(hx[k], lx[k]);
-			out[R + r0 + k * 32] = make_float2(hy[k], ly[k]);
-			out[2 * R + r0 + k * 32] = make_float2(hz[k], lz[k]);
+			if (SS) {
+				out[r0 + k * 32] = csum[0][SS ? k : 0][SS ? tid : 0];
+				out[R + r0 + k * 32] = csum[SS ? 1 : 0][SS ? k : 0][SS ? tid : 0];
+				out[2 * R + r0 + k * 32] = csum[SS ? 2 : 0][SS ? k : 0][SS ? tid : 0];
+			} else {
+				out[r0 + k * 32] = make_float2(hx[k], lx[k]);
+				out[R + r0 + k * 32] = make_float2(hy[k], ly[k]);
+				out[2 * R + r0 + k * 32] = make_float2(hz[k], lz[k]);
+			}
 		}
 		ub = S.unit_begin + t1;
 		++s;
@@ -273,10 +370,13 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 // launched the ordinary way (not as a programmatic dependent): see the kernel's prologue
 #define GRAV_SYM_ENTRY(B, W, J) \
 	{GRAV_MODE_FP32U, B, 32 * W, J, \
-		reinterpret_cast<const void*>(&stage1_sym_kernel<B, W, J, 4, 1>), 2 * J * 16, false}
+		reinterpret_cast<const void*>(&stage1_sym_kernel<B, W, J, 4, SYM_PLAIN>), 2 * J * 16, false}
 #define GRAV_SYMC_ENTRY(B, W, J) \
 	{GRAV_MODE_FP32CU, B, 32 * W, J, \
-		reinterpret_cast<const void*>(&stage1_sym_kernel<B, W, J, 4, 2>), 2 * 2 * J * 16, false}
+		reinterpret_cast<const void*>(&stage1_sym_kernel<B, W, J, 4, SYM_DS>), 2 * 2 * J * 16, false}
+#define GRAV_SYMN_ENTRY(B, W, J) \
+	{GRAV_MODE_FP32UN, B, 32 * W, J, \
+		reinterpret_cast<const void*>(&stage1_sym_kernel<B, W, J, 4, SYM_NEAR>), 2 * 2 * J * 16, false}
 
 static const Stage1Kernel k_table_sym[] = {
 	GRAV_SYM_ENTRY(4, 4, 128),
@@ -291,6 +391,12 @@ static const Stage1Kernel k_table_sym[] = {
 	GRAV_SYMC_ENTRY(8, 4, 256),
 	GRAV_SYMC_ENTRY(4, 4, 256),
 	GRAV_SYMC_ENTRY(4, 8, 256),
+	GRAV_SYMN_ENTRY(4, 4, 128),
+	GRAV_SYMN_ENTRY(8, 4, 256),
+	GRAV_SYMN_ENTRY(8, 4, 128),
+	GRAV_SYMN_ENTRY(8, 4, 64),
+	GRAV_SYMN_ENTRY(4, 4, 256),
+	GRAV_SYMN_ENTRY(4, 8, 256),
 };
 
 int stage1_table_sym(const Stage1Kernel** out)

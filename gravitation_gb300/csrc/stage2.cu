@@ -26,6 +26,13 @@ constexpr int SPLIT_ROWS_MAX = 32768;  // TPR = 4 up to this many padded rows, e
 constexpr int ROW_BATCH = 8;           // FP64 row-slot loads in flight per lane
 constexpr int COL_BATCH = 16;          // FP32 column-slot loads in flight per lane
 
+// modes whose stage 1 reads the low parts of the positions (second float4 array)
+__device__ __forceinline__ bool has_lo(int mode)
+{
+	return mode == GRAV_MODE_FP32C || mode == GRAV_MODE_FP32CU || mode == GRAV_MODE_FP32N ||
+		mode == GRAV_MODE_FP32UN;
+}
+
 template <int TPR>
 __global__ void __launch_bounds__(S2_THREADS) stage2_kernel(const grav_batch b, const int flags)
 {
@@ -55,8 +62,7 @@ __global__ void __launch_bounds__(S2_THREADS) stage2_kernel(const grav_batch b, 
 		} else {
 			float4* q = static_cast<float4*>(b.pos);
 			q[g] = make_float4(0.f, 0.f, 0.f, 0.f);
-			if (b.mode == GRAV_MODE_FP32C || b.mode == GRAV_MODE_FP32CU)
-				q[b.n_pad_total + g] = make_float4(0.f, 0.f, 0.f, 0.f);
+			if (has_lo(b.mode)) q[b.n_pad_total + g] = make_float4(0.f, 0.f, 0.f, 0.f);
 		}
 		return;
 	}
@@ -77,7 +83,8 @@ __global__ void __launch_bounds__(S2_THREADS) stage2_kernel(const grav_batch b, 
 		const int64_t stride = 3 * static_cast<int64_t>(IT);  // 8-byte entries per slot
 		// unique-pair plans: the last (row block index) slots of a segment are column
 		// slots holding FP32 sums in their first half (stage1_sym.cu)
-		const bool pairs = b.mode == GRAV_MODE_FP32U || b.mode == GRAV_MODE_FP32CU;
+		const bool pairs = b.mode == GRAV_MODE_FP32U || b.mode == GRAV_MODE_FP32CU ||
+			b.mode == GRAV_MODE_FP32UN;
 		const int nrow = pairs ? S.nslots - S.il0 / IT : S.nslots;
 		if (b.mode == GRAV_MODE_FP64) {
 			// FP64 row slots p, p + TPR, ... added in order; each round issues all its
@@ -209,7 +216,7 @@ __global__ void __launch_bounds__(S2_THREADS) stage2_kernel(const grav_batch b, 
 		const float hy = __double2float_rn(r.y);
 		const float hz = __double2float_rn(r.z);
 		q[g] = make_float4(hx, hy, hz, __double2float_rn(r.w));
-		if (b.mode == GRAV_MODE_FP32C || b.mode == GRAV_MODE_FP32CU) {
+		if (has_lo(b.mode)) {
 			q[b.n_pad_total + g] = make_float4(
 				__double2float_rn(__dsub_rn(r.x, static_cast<double>(hx))),
 				__double2float_rn(__dsub_rn(r.y, static_cast<double>(hy))),
@@ -218,7 +225,7 @@ __global__ void __launch_bounds__(S2_THREADS) stage2_kernel(const grav_batch b, 
 	}
 }
 
-cudaError_t launch_stage2(const grav_batch& b, int flags, cudaStream_t stream)
+cudaError_t launch_stage2(const grav_batch& b, int flags, cudaStream_t stream, bool dependent)
 {
 	if (b.n_pad_total == 0) return cudaSuccess;
 	const int tpr = b.n_pad_total <= SPLIT_ROWS_MAX ? 4 : 1;
@@ -228,6 +235,9 @@ cudaError_t launch_stage2(const grav_batch& b, int flags, cudaStream_t stream)
 	void* args[] = {&copy, &f};
 	const void* fn = tpr == 4 ? reinterpret_cast<const void*>(&stage2_kernel<4>)
 	                          : reinterpret_cast<const void*>(&stage2_kernel<1>);
+	if (!dependent)
+		return cudaLaunchKernel(fn, dim3(static_cast<unsigned>(blocks)), dim3(S2_THREADS), args,
+			0, stream);
 	return launch_dependent(fn, static_cast<unsigned>(blocks), S2_THREADS, 0, stream, args);
 }
 

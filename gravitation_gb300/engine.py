@@ -8,7 +8,8 @@ stream.  There is no CPU path: without the library or a GB300 every call raises.
 Layout in HBM (all packed universe after universe):
   r, v     float64 [n_bodies, 4]   (x, y, z, G*m) and (vx, vy, vz, 0); or, after
            bind_host_state, the caller's pinned host tensors of that layout
-  pos      padded stage-1 positions: float4 hi (+ float4 lo in fp32c/fp32cu) or double4
+  pos      padded stage-1 positions: float4 hi (+ float4 lo in fp32c/fp32cu/fp32n/fp32un)
+           or double4
   part     8-byte entries [n_slots, 3, itile]  partial sums written by stage 1: FP32
            (hi, lo) pairs in the row slots (FP64 values in fp64 mode); the unique-pair
            column slots hold FP32 sums in their first half
@@ -78,7 +79,8 @@ def occupancy(mode, tile, device=None):
 
 def make_plan(sizes, T, tile, mode='fp32'):
     """Host-side plan (no GPU needed): (PlanInfo, univ ctypes array, seg ctypes array).
-    The unique-pair mode (fp32u) uses grav_plan_pairs, every other mode grav_plan."""
+    The unique-pair modes (fp32u, fp32cu, fp32un) use grav_plan_pairs, the others
+    grav_plan."""
     L = _lib.load()
     fn = L.grav_plan_pairs if mode in _lib.PAIR_MODES else L.grav_plan
     sizes = [int(x) for x in sizes]
@@ -188,8 +190,9 @@ class Engine:
     Parameters
       sizes : list of body counts (one per universe)
       T     : time step (scalar or one per universe)
-      mode  : 'fp32' (default, all pairs), 'fp32u' (unique pairs), 'fp32c' / 'fp32cu'
-              (compensated positions) or 'fp64'
+      mode  : 'fp32' (default, all pairs), 'fp32u' (unique pairs), 'fp32n' / 'fp32un'
+              (near pairs from double-single separations), 'fp32c' / 'fp32cu'
+              (double-single separations for every pair) or 'fp64'
       tile  : _lib.Tile, or None to use the autotuner's choice / the default shape
     """
 

@@ -16,12 +16,14 @@ Behaviour seen from the front end (README.md:50, worker.py:119-136):
     kernels re-read pm._r every stage 1 (np1.py:101-102, pc2.py:147-151).
 
 Kernel options (keyword arguments of the constructor, kept in self._meta):
-  precision  'fp32' | 'fp32u' | 'fp32c' | 'fp32cu' | 'fp64'   default from dtype:
-             'float32' -> fp32 below 8192 bodies, fp32u from there on while its
-             partial-sum slots fit an eighth of the GPU's memory (~1.7 M bodies);
-             'float64' -> fp64.  fp32/fp32u share the FP32 arithmetic (fp32u visits each pair
-             once); fp32c/fp32cu add the low parts of the positions (separations
-             exact to FP32 precision anywhere in space)
+  precision  'fp32n' | 'fp32un' | 'fp32' | 'fp32u' | 'fp32c' | 'fp32cu' | 'fp64'   default
+             from dtype: 'float32' -> fp32n below 8192 bodies, fp32un from there on while
+             its partial-sum slots fit an eighth of the GPU's memory (~1.7 M bodies);
+             'float64' -> fp64.  fp32/fp32u: plain FP32 separations (fp32u visits each
+             pair once); fp32n/fp32un: the same plus double-single separations for near
+             pairs (closer than |x|/20), which keeps every body within ~1e-6 of the FP64
+             forces wherever the bodies are; fp32c/fp32cu: double-single separations for
+             every pair
   host_sync  'full' (upload + download every step) | 'pull' (download only) |
              'none' (device state only; call sync_host() to refresh the mirror)
   fuse       True (default): stage 1 and stage 2 both run in step_stage1 on the GPU
@@ -50,10 +52,11 @@ import torch
 from . import _lib, generate
 from .engine import Engine
 
-# float32 runs the FP32 arithmetic either on unique pairs (fp32u: each pair once, like
-# the reference's CPU kernels; faster from ~8k bodies on) or on all ordered pairs (fp32:
-# finer work units, faster for small universes); the results agree to FP32 rounding
-_DTYPE_MODE = {'float32': 'fp32', 'float64': 'fp64'}
+# float32 runs the FP32 arithmetic with near pairs corrected, either on unique pairs
+# (fp32un: each pair once, like the reference's CPU kernels; faster from ~8k bodies on)
+# or on all ordered pairs (fp32n: finer work units, faster for small universes); the
+# results agree to FP32 rounding
+_DTYPE_MODE = {'float32': 'fp32n', 'float64': 'fp64'}
 UNIQUE_PAIRS_FROM_N = 8192
 
 
@@ -63,10 +66,10 @@ def default_mode(dtype, n, budget=None):
     slot budget (engine.slot_budget_bytes, or `budget` bytes), on all pairs otherwise
     (above ~1.7 million bodies on a GB300)."""
     mode = _DTYPE_MODE.get(str(dtype))
-    if mode == 'fp32' and n >= UNIQUE_PAIRS_FROM_N:
+    if mode == 'fp32n' and n >= UNIQUE_PAIRS_FROM_N:
         from .engine import pair_plan_fits
-        if pair_plan_fits([n], budget):
-            mode = 'fp32u'
+        if pair_plan_fits([n], budget, mode='fp32un'):
+            mode = 'fp32un'
     return mode
 
 

@@ -2,7 +2,10 @@
 
 For a workload key -- the GPU (name, SM count), the precision mode, the library's
 source hash and the size bucket (single universe: N rounded up to a power of two;
-batch: a signature of the size list) -- every compiled tile shape, at 1, 1/2 and 1/4 of
+batch: the size classes of its universe count and of its largest universe and the
+binary order of magnitude of its sum of N^2, so that batches of the same make-up share
+a tuned tile whatever their exact sizes) -- every compiled
+tile shape, at 1, 1/2 and 1/4 of
 the resident persistent grid, is timed as full steps replayed from a CUDA graph (CUDA
 events, at least ~2 ms of steps) on a seeded synthetic state of that size, and the
 fastest is cached as JSON.
@@ -14,7 +17,6 @@ not compiled are ignored, and nothing is trusted that does not pass
 gravitation_gb300/_tune_cache.json.
 """
 
-import hashlib
 import json
 import os
 import tempfile
@@ -28,13 +30,24 @@ from .build import source_hash
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
+def size_class(n):
+    """Power-of-two class of a universe size: the smallest 2^k >= n (0 for no bodies)."""
+    n = int(n)
+    return 0 if n <= 0 else 1 << (n - 1).bit_length()
+
+
 def bucket_of(sizes):
+    """Tuner key of a size list.  One universe: its size class.  A batch: the size class
+    of its universe count, the binary order of magnitude of its work (sum of N^2) and
+    the size class of its largest universe, e.g. 'batch:u256:w32:max16384' -- what the
+    tile choice depends on -- so that batches drawn from one distribution (other seeds
+    of the same log-uniform range) share their tuned tile."""
     sizes = [int(s) for s in sizes]
     if len(sizes) == 1:
-        n = max(sizes[0], 1)
-        return 'single:%d' % (1 << (n - 1).bit_length())
-    h = hashlib.sha1(np.asarray(sorted(sizes), dtype=np.int64).tobytes()).hexdigest()[:12]
-    return 'batch:%d:%s' % (len(sizes), h)
+        return 'single:%d' % size_class(max(sizes[0], 1))
+    work = sum(n * n for n in sizes)
+    return 'batch:u%d:w%d:max%d' % (size_class(len(sizes)), max(work, 1).bit_length() - 1,
+                                    size_class(max(sizes + [0])))
 
 
 class Tuner:

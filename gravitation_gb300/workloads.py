@@ -155,7 +155,7 @@ def run_adjoint_check(n=4096, steps=1000, every=32, seed=3, ncoords=16, eps=1e-6
 
 
 def run_precision(n=16384, steps=10000, every=100, seed=2,
-                  modes=('fp32u', 'fp32cu', 'fp32c', 'fp64'),
+                  modes=('fp32u', 'fp32un', 'fp32cu', 'fp32c', 'fp64'),
                   sample=256, check=None, device=None):
     """Precision stress: two Plummer spheres (scale radius 50, centres 1000 apart,
     approaching at 5 along x, masses log-uniform in [0.1, 1000]).  For each mode: the
@@ -214,7 +214,7 @@ def run_precision(n=16384, steps=10000, every=100, seed=2,
     return out
 
 
-def run_sweep(sizes=None, mode='fp32u', reps=5, tuner=None, device=None):
+def run_sweep(sizes=None, mode='fp32un', reps=5, tuner=None, device=None):
     """Interactions/s of the single-universe step over an N sweep (2^4 .. 2^17)."""
     from .scenarios import uniform_cube
     sizes = sizes or [2 ** k for k in range(4, 18)]

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define GRAV_ABI_VERSION 3
+#define GRAV_ABI_VERSION 4
 
 /* status codes */
 #define GRAV_OK 0
@@ -54,6 +54,19 @@ extern "C" {
                                  once, both bodies updated); plan with grav_plan_pairs */
 #define GRAV_MODE_FP32CU 4    /* GRAV_MODE_FP32C's double-single positions on unique pairs;
                                  plan with grav_plan_pairs */
+#define GRAV_MODE_FP32N 5     /* GRAV_MODE_FP32 with near pairs corrected: every pair closer
+                                 than max|x_i| / GRAV_NEAR_KAPPA (max over the coordinates of
+                                 the rows a thread holds) is evaluated from the double-single
+                                 separation (hi_j - hi_i) + (lo_j - lo_i) instead of the FP32
+                                 one; a pair whose FP32 separation is exactly zero contributes
+                                 nothing, as in GRAV_MODE_FP32 */
+#define GRAV_MODE_FP32UN 6    /* GRAV_MODE_FP32N's correction on unique pairs; plan with
+                                 grav_plan_pairs */
+
+/* Near-pair radius of GRAV_MODE_FP32N / GRAV_MODE_FP32UN in units of the coordinate
+ * magnitude: beyond |x| / 20 the FP32 rounding of the positions changes a pair term by
+ * at most ~4.5e-6 of itself. */
+#define GRAV_NEAR_KAPPA 20
 
 /* stage-2 flags */
 #define GRAV_S2_INTEGRATE 1   /* v = a*T + v ; r = v*T + r */
@@ -172,7 +185,8 @@ int grav_plan_pairs(int32_t n_univ, const int32_t* n, const double* T, const gra
 /* Bytes of the padded stage-1 position array for `mode` and `n_pad_total` rows. */
 int64_t grav_pos_bytes(int mode, int64_t n_pad_total);
 
-/* Bytes of the FP64 partial-sum buffer for a plan. */
+/* Bytes of the partial-sum buffer (grav_batch.part) for a plan: 3 x itile 8-byte entries
+ * per slot. */
 int64_t grav_part_bytes(const grav_plan_info* info);
 
 /* r^2 floor for the FP32 modes: max(1e-25, (max_gm / 1e36)^(2/3)), the smallest value
@@ -188,7 +202,8 @@ float grav_eps2(double max_gm);
 int grav_prepare(const grav_batch* b, void* stream);
 
 /*
- * Stage 1: FP64 partial sums of the accelerations into b->part.
+ * Stage 1: partial sums of the accelerations into b->part (FP32 (hi, lo) compensated
+ * pairs per row and FP32 column sums in the FP32 modes, FP64 values in GRAV_MODE_FP64).
  * Replaces universe_base.step_stage1 (_base_.py:147-150) as realised by
  * np1.update_pair/step_stage1 (np1.py:81-108), c1a's step_stage1
  * (_lib1_/lib.c:52-126) and pc2.update_all (pc2.py:59-91).
@@ -196,7 +211,8 @@ int grav_prepare(const grav_batch* b, void* stream);
 int grav_stage1(const grav_batch* b, void* stream);
 
 /*
- * Stage 2: sum the partials (FP64), optionally write a_out, optionally integrate
+ * Stage 2: sum the partials (compensated FP32 in the FP32 modes, widened to FP64 once per
+ * body; FP64 in GRAV_MODE_FP64), optionally write a_out, optionally integrate
  * (v = a*T + v; r = v*T + r in FP64, no fused multiply-add, as _base_.py:58-62 and
  * np2.py:110-115), then refresh the padded stage-1 positions.
  * Replaces universe_base.step_stage2 (_base_.py:152-156) / np2.step_stage2.
@@ -276,12 +292,17 @@ int grav_adjoint_step(const grav_adjoint* a, void* stream);
  * work is captured or timed, hosts that reserve all device memory up front).
  * Inputs: r, n x 4 doubles (x, y, z, G*m) on the device; max_gm = the largest G*m
  * (sets the FP32 r^2 floor, see grav_eps2).  Output: a, n x 4 doubles (ax, ay, az, 0).
- * err: optional device int (GRAV_DEV_* written by the kernels; NULL = internal).
+ * err: optional device int that the kernels set to a GRAV_DEV_* code when a bounded
+ * wait expires (first error wins); the call never clears it, so the caller zeroes it
+ * before the first call and may share it with other work.  With err = NULL the kernels
+ * use an internal flag that no caller can read: a device-side timeout then goes
+ * unreported (the accelerations of that call are incomplete), so pass a flag wherever
+ * that matters.
  * Same arithmetic as grav_stage1 + grav_stage2(GRAV_S2_WRITE_A) in GRAV_MODE_FP32, on a
  * fixed tile (2 bodies/thread, 128 threads, 128-body j-tiles).
  * It calls no cudaMalloc/cudaFree or other allocating routine: its scratch (plan
- * tables, padded positions, FP64 partial sums, error flag) is one file-scope device
- * array of about 3.8 MB that every GPU loading the library holds until exit.  The first
+ * tables, padded positions, FP32 (hi, lo) partial sums, error flag) is one file-scope
+ * device array of about 3.8 MB that every GPU loading the library holds until exit.  The first
  * call on each device, with that device current, looks up the array's device address
  * (cudaGetSymbolAddress); make that first call before any stream capture.  Every call
  * shares the array: calls whose work overlaps on the GPU race.  n above the limit is

@@ -30,7 +30,10 @@ import sysconfig
 import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get('GRAVITATION_REFERENCE', '/root/reference')
+# the reference's source tree: $GRAVITATION_REFERENCE, else where this build recipe
+# finds it in the development container (absent on the GPU host, where only the builds
+# made from it travel)
+REF_ROOT = os.environ.get('GRAVITATION_REFERENCE') or '/root/reference'
 REF_KERNEL = os.path.join(REF_ROOT, 'src', 'gravitation', 'kernel')
 
 

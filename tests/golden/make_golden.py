@@ -17,7 +17,8 @@ gravitation/kernel/), on seeded inputs:
 Inputs follow the uniform-cube workload: r ~ U[-1000,1000]^3, v ~ N(0,1), m ~ U[1,100]
 (numpy default_rng(seed)), G, T and scaling at universe_base defaults.
 
-Usage: python tests/golden/make_golden.py [--ref /root/reference]
+Usage: python tests/golden/make_golden.py [--ref REFERENCE_TREE]
+(default: $GRAVITATION_REFERENCE, else the tree oracle/build.py builds from)
 """
 
 import argparse
@@ -55,7 +56,9 @@ def run_kernel(mod, r, v, m, steps, dtype, record_a=(), **uni_kw):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--ref', default=os.environ.get('GRAVITATION_REFERENCE', '/root/reference'))
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))))
+    from oracle.build import REF_ROOT
+    ap.add_argument('--ref', default=REF_ROOT)
     args = ap.parse_args()
     sys.path.insert(0, os.path.join(args.ref, 'src'))
     import importlib

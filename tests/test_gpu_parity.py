@@ -2,11 +2,13 @@
 reference's golden vectors.
 
 Tolerances (relative per-body acceleration error |a - a_ref| / |a_ref|):
-  fp32   1e-5 against the FP64 oracle evaluated on the FP32-rounded positions the
-         kernel reads (arithmetic error), as the reference's own FP32 kernels
-         (np1/np2) are measured from identical states
-  fp32c  1e-5 against the FP64 oracle on the FP64 state itself
-  fp64   1e-12 against the FP64 oracle on the FP64 state
+  fp32, fp32u    1e-5 against the FP64 oracle evaluated on the FP32-rounded positions
+                 the kernel reads (arithmetic error), as the reference's own FP32
+                 kernels (np1/np2) are measured from identical states
+  fp32n, fp32un  1e-5 against the FP64 oracle on the FP64 state itself (the plugin's
+                 float32 default: near pairs from double-single separations)
+  fp32c, fp32cu  1e-5 against the FP64 oracle on the FP64 state itself
+  fp64           1e-12 against the FP64 oracle on the FP64 state
 Stage 2 is bit-exact against the FP64 update of _base_.py:58-62.
 """
 
@@ -21,7 +23,9 @@ from gravitation_gb300.scenarios import G_DEFAULT, uniform_cube, plummer_pair
 
 pytestmark = pytest.mark.gpu
 
-TOL = {'fp32': 1e-5, 'fp32u': 1e-5, 'fp32c': 1e-5, 'fp32cu': 1e-5, 'fp64': 1e-12}
+TOL = {'fp32': 1e-5, 'fp32u': 1e-5, 'fp32n': 1e-5, 'fp32un': 1e-5, 'fp32c': 1e-5,
+       'fp32cu': 1e-5, 'fp64': 1e-12}
+ALL_MODES = ['fp32', 'fp32u', 'fp32n', 'fp32un', 'fp32c', 'fp32cu', 'fp64']
 
 
 def r32(r):
@@ -44,7 +48,7 @@ def engine_forces(mode, r, v, m, G=G_DEFAULT, tile=None):
     return a, eng
 
 
-@pytest.mark.parametrize('mode', ['fp32', 'fp32u', 'fp32c', 'fp32cu', 'fp64'])
+@pytest.mark.parametrize('mode', ALL_MODES)
 @pytest.mark.parametrize('n', [1, 2, 3, 31, 33, 127, 129, 257, 1000])
 def test_forces_small_n(gpu, mode, n):
     r, v, m = uniform_cube(n, seed=100 + n)
@@ -57,14 +61,17 @@ def test_forces_small_n(gpu, mode, n):
     assert err.max() < TOL[mode], (mode, n, err.max())
 
 
-@pytest.mark.parametrize('mode', ['fp32', 'fp32u', 'fp32c', 'fp32cu', 'fp64'])
+@pytest.mark.parametrize('mode', ALL_MODES)
 def test_every_tile_shape(gpu, mode):
     n = 777
     r, v, m = uniform_cube(n, seed=7)
     ref = oracle_accel(mode, r, m, G_DEFAULT)
     for t in tile_list(mode):
         for grid in (1, 3, 1000):
-            a, _ = engine_forces(mode, r, v, m, tile=_lib.Tile(t.bpt, t.threads, t.jtile, grid))
+            try:
+                a, _ = engine_forces(mode, r, v, m, tile=_lib.Tile(t.bpt, t.threads, t.jtile, grid))
+            except _lib.GravError as e:
+                raise AssertionError('%s tile %r grid %d: %s' % (mode, t, grid, e)) from e
             err = oracle.rel_err_per_body(a, ref).max()
             assert err < TOL[mode], (mode, t, grid, err)
 
@@ -144,20 +151,46 @@ def test_stage2_bit_exact(gpu, mode):
 
 
 def test_full_size_sampled_65536(gpu):
-    """N = 65536: sampled bodies against the FP64 oracle, all three modes."""
+    """N = 65536: sampled bodies against the FP64 oracle, every FP32 mode."""
     n = 65536
     r, v, m = uniform_cube(n, seed=0)
     rows = np.random.default_rng(9).choice(n, 192, replace=False)
-    for mode in ('fp32', 'fp32u', 'fp32c', 'fp32cu'):
+    for mode in ('fp32', 'fp32u', 'fp32n', 'fp32un', 'fp32c', 'fp32cu'):
         a, _ = engine_forces(mode, r, v, m)
         ref = oracle_accel(mode, r, m, G_DEFAULT, rows=rows)
         err = oracle.rel_err_per_body(a[rows], ref)
         assert err.max() < 1e-5, (mode, err.max())
-    # the plain mode's error on the FP64 state itself includes the rounding of the
-    # positions to FP32; it is reported, bounded loosely here
-    a, _ = engine_forces('fp32', r, v, m)
-    ref = oracle.accel_fp64(r, G_DEFAULT * m, 1.0, rows=rows)
-    assert oracle.rel_err_per_body(a[rows], ref).max() < 2e-4
+
+
+def fp64_forces_gpu(r, m):
+    """Every body's acceleration in the GPU FP64 mode (itself pinned to the oracle at
+    1e-12 by the small-N, golden-vector and sampled tests of this module)."""
+    a, _ = engine_forces('fp64', r, np.zeros_like(r), m)
+    return a
+
+
+@pytest.mark.parametrize('mode,n,seed', [('fp32un', 65536, 0), ('fp32n', 8192, 0),
+                                         ('fp32n', 4096, 3), ('fp32un', 16384, 1)])
+def test_default_float32_every_body_fp64_state(gpu, mode, n, seed):
+    """The plugin's float32 default (fp32n below 8192 bodies, fp32un from there) on the
+    FP64 state itself: every body within 1e-5 of the FP64 forces (bodies of the uniform
+    cube sit up to 1000 from the origin, where rounding a coordinate to FP32 moves it by
+    up to 3e-5: the plain FP32 modes exceed 1e-5 on ~0.2 % of the bodies there)."""
+    r, v, m = uniform_cube(n, seed=seed)
+    a64 = fp64_forces_gpu(r, m)
+    rows = np.random.default_rng(seed + 5).choice(n, 16, replace=False)
+    ref = oracle.accel_fp64(r, G_DEFAULT * m, 1.0, rows=rows, coincident=True)
+    assert oracle.rel_err_per_body(a64[rows], ref).max() < 1e-12
+    a, eng = engine_forces(mode, r, v, m)
+    err = oracle.rel_err_per_body(a, a64)
+    assert err.max() < 1e-5, (mode, n, err.max(), int((err > 1e-5).sum()))
+    assert np.array_equal(eng.forces().cpu().numpy(), a)     # deterministic
+    # the plain FP32 mode of the same arithmetic, for contrast: only its tail is wrong
+    plain = {'fp32un': 'fp32u', 'fp32n': 'fp32'}[mode]
+    a_plain, _ = engine_forces(plain, r, v, m)
+    e_plain = oracle.rel_err_per_body(a_plain, a64)
+    assert np.median(e_plain) < 1e-5
+    assert err.max() <= e_plain.max()
 
 
 def test_size_independent_properties_65536(gpu):
@@ -201,7 +234,7 @@ def test_plummer_pair_precision_modes(gpu):
     n = 4096
     r, v, m = plummer_pair(n, seed=2)
     rows = np.arange(0, n, 16)
-    for mode in ('fp32', 'fp32u', 'fp32c', 'fp32cu', 'fp64'):
+    for mode in ALL_MODES:
         a, _ = engine_forces(mode, r, v, m)
         ref = oracle_accel(mode, r, m, G_DEFAULT, rows=rows)
         err = oracle.rel_err_per_body(a[rows], ref).max()
@@ -219,7 +252,7 @@ def test_edge_cases(gpu):
     # coincident bodies exert no force on each other (the reference gives inf/nan)
     r = np.array([[0.0, 0, 0], [1.0, 0, 0], [1.0, 0, 0]])
     m = np.ones(3) / G_DEFAULT
-    for mode in ('fp32', 'fp32u', 'fp32c', 'fp32cu', 'fp64'):
+    for mode in ALL_MODES:
         a, _ = engine_forces(mode, r, np.zeros((3, 3)), m)
         assert np.all(np.isfinite(a))
         assert np.allclose(a[1], [-1.0, 0, 0], rtol=1e-6)
@@ -228,11 +261,31 @@ def test_edge_cases(gpu):
     # unique-pair kernel, so they meet on its unique-pair path, not the diagonal one)
     r, v, m = uniform_cube(5000, seed=31)
     r[4321] = r[7]
-    for mode in ('fp32', 'fp32u', 'fp32c', 'fp32cu', 'fp64'):
+    for mode in ALL_MODES:
         a, _ = engine_forces(mode, r, v, m)
         assert np.all(np.isfinite(a)), mode
         ref = oracle_accel(mode, r, m, G_DEFAULT, rows=np.array([7, 4321, 0]))
         assert oracle.rel_err_per_body(a[[7, 4321, 0]], ref).max() < TOL[mode], mode
+    # two bodies 1e-3 apart at x = 1000, where FP32 resolves 6.1e-5: the near modes
+    # take their separation from the double-single positions (within FP32 rounding of the
+    # exact force); the plain modes see the FP32-rounded separation
+    r = np.array([[1000.0, 0, 0], [1000.001, 0, 0], [-1000.0, 0.0, 0]])
+    m = np.array([1.0, 2.0, 3.0]) / G_DEFAULT
+    ref = oracle.accel_fp64(r, G_DEFAULT * m, 1.0, coincident=True)
+    for mode in ('fp32n', 'fp32un', 'fp32c', 'fp32cu'):
+        a, _ = engine_forces(mode, r, np.zeros((3, 3)), m)
+        assert oracle.rel_err_per_body(a, ref).max() < 1e-5, mode
+    a, _ = engine_forces('fp32', r, np.zeros((3, 3)), m)
+    assert oracle.rel_err_per_body(a, ref)[:2].max() > 1e-3
+    # closer than the FP32 resolution of their coordinates: the FP32 separation is
+    # exactly zero, and such a pair contributes nothing in every FP32 mode but the
+    # double-single ones
+    r = np.array([[1000.0, 0, 0], [1000.00001, 0, 0], [0.0, 10.0, 0]])
+    ref = oracle.accel_fp64(r32(r), G_DEFAULT * m, 1.0, coincident=True)
+    for mode in ('fp32n', 'fp32un', 'fp32', 'fp32u'):
+        a, _ = engine_forces(mode, r, np.zeros((3, 3)), m)
+        assert np.all(np.isfinite(a)), mode
+        assert oracle.rel_err_per_body(a, ref).max() < 1e-5, mode
     # massless bodies feel forces but exert none
     r, v, m = uniform_cube(100, seed=3)
     m[::3] = 0.0
@@ -248,7 +301,7 @@ def test_batched_matches_single(gpu):
     """Several universes in one persistent launch == each universe alone."""
     sizes = [64, 1000, 3, 4096, 517]
     rs, vs, ms = zip(*[uniform_cube(n, seed=50 + i) for i, n in enumerate(sizes)])
-    for mode in ('fp32', 'fp32u', 'fp64'):
+    for mode in ('fp32', 'fp32u', 'fp32n', 'fp32un', 'fp64'):
         eng = Engine(sizes, [1e3] * len(sizes), mode=mode)
         eng.set_state(np.concatenate(rs), np.concatenate(vs), G_DEFAULT * np.concatenate(ms))
         a = eng.forces().cpu().numpy()
@@ -260,7 +313,7 @@ def test_batched_matches_single(gpu):
         eng.raise_on_device_error()
 
 
-@pytest.mark.parametrize('mode', ['fp32', 'fp32u', 'fp32c', 'fp32cu', 'fp64'])
+@pytest.mark.parametrize('mode', ALL_MODES)
 def test_empty_and_ragged_batches(gpu, mode):
     """Universes without bodies anywhere in a batch (first, between, last) take no rows
     and leave the others' answers unchanged; batches of nothing but empty universes step
@@ -295,7 +348,7 @@ def test_empty_and_ragged_batches(gpu, mode):
         e.raise_on_device_error()
 
 
-@pytest.mark.parametrize('mode', ['fp32u', 'fp32'])
+@pytest.mark.parametrize('mode', ['fp32u', 'fp32', 'fp32un'])
 def test_maximum_size_2_20(gpu, mode):
     """N = 2^20 bodies in one universe (one step is 1.1e12 interactions; the unique-pair
     plan holds ~525k partial-sum slots): sampled bodies against the FP64 oracle, the
@@ -359,15 +412,16 @@ def test_energy_momentum_fp64(gpu):
         assert np.all(np.isfinite(out2))
 
 
-def test_graph_replay_matches_launches(gpu):
+@pytest.mark.parametrize('mode', ['fp32', 'fp32n', 'fp32un'])
+def test_graph_replay_matches_launches(gpu, mode):
     """The CUDA-graph step replays exactly what the launched steps compute."""
-    sizes = [300, 64, 2000]
+    sizes = [300, 64, 2000, 9000]
     rs, vs, ms = zip(*[uniform_cube(n, seed=90 + i) for i, n in enumerate(sizes)])
     r, v, gm = np.concatenate(rs), np.concatenate(vs), G_DEFAULT * np.concatenate(ms)
-    a = Engine(sizes, 1e3, mode='fp32')
+    a = Engine(sizes, 1e3, mode=mode)
     a.set_state(r, v, gm)
     a.step(4)
-    b = Engine(sizes, 1e3, mode='fp32', tile=a.tile)
+    b = Engine(sizes, 1e3, mode=mode, tile=a.tile)
     b.set_state(r, v, gm)
     g = b.capture_graph(2)
     g.replay()

@@ -131,7 +131,7 @@ def test_frontend_protocol_workload(gpu):
     assert [r['n'] for r in out['sizes']] == [64, 128, 256, 512]
     for r in out['sizes']:
         assert r['steps'] >= 3 and 0 < r['best_ns'] <= r['avg_ns']
-        assert r['mode'] == 'fp32'
+        assert r['mode'] == 'fp32n'   # the float32 default below 8192 bodies
 
 
 @pytest.mark.parametrize('sync', ['full', 'pull', 'none'])

@@ -15,7 +15,7 @@ from gravitation_gb300.tune import Tuner
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize('mode,n', [('fp32', 3000), ('fp32u', 9000)])
+@pytest.mark.parametrize('mode,n', [('fp32', 3000), ('fp32u', 9000), ('fp32n', 3000), ('fp32un', 9000)])
 def test_tune_caches_a_valid_choice(gpu, tmp_path, mode, n):
     info = device_info(0)
     t = Tuner(str(tmp_path / 'cache.json'))

@@ -15,7 +15,7 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GB1 = os.path.join(ROOT, 'gravitation_gb300', 'kernel', 'gb1')
-REF = os.environ.get('GRAVITATION_REFERENCE', '/root/reference')
+from oracle.build import REF_ROOT as REF  # noqa: E402  (the reference tree, if present)
 REF_SRC = os.path.join(REF, 'src')
 META = ('longname', 'version', 'description', 'requirements', 'externalrequirements',
         'interpreters', 'parallel', 'license', 'authors')
@@ -220,8 +220,8 @@ def test_default_precision_by_dtype_and_size():
     from gravitation_gb300.engine import plan_part_bytes, tile_list
     from gravitation_gb300 import _lib
     gib = 1 << 30
-    assert default_mode('float32', 1024) == 'fp32'
-    assert default_mode('float32', 65536) == 'fp32u'
+    assert default_mode('float32', 1024) == 'fp32n'
+    assert default_mode('float32', 65536) == 'fp32un'
     assert default_mode('float64', 65536) == 'fp64'
     assert default_mode('float16', 10) is None
     # the unique-pair slots grow as N^2 / rows-per-block; the all-pairs slots do not
@@ -231,10 +231,10 @@ def test_default_precision_by_dtype_and_size():
     assert plan_part_bytes([1 << 22], t, 'fp32u') > 15 * plan_part_bytes([1 << 20], t, 'fp32u')
     assert plan_part_bytes([4096], t, 'fp32u', comps=7) * 3 == plan_part_bytes([4096], t, 'fp32u') * 7
     # beyond the slot budget float32 falls back to all pairs (forward and backward)
-    worst = max(plan_part_bytes([1 << 20], x, 'fp32u') for x in tile_list('fp32u'))
-    assert default_mode('float32', 1 << 20, budget=worst) == 'fp32u'
-    assert default_mode('float32', 1 << 20, budget=worst - 1) == 'fp32'
-    assert default_mode('float32', 1 << 23, budget=32 * gib) == 'fp32'
+    worst = max(plan_part_bytes([1 << 20], x, 'fp32un') for x in tile_list('fp32un'))
+    assert default_mode('float32', 1 << 20, budget=worst) == 'fp32un'
+    assert default_mode('float32', 1 << 20, budget=worst - 1) == 'fp32n'
+    assert default_mode('float32', 1 << 23, budget=32 * gib) == 'fp32n'
     assert default_adjoint_pairs([4096], budget=32 * gib)
     assert not default_adjoint_pairs([4096], budget=1)
     assert not default_adjoint_pairs([1 << 22], budget=32 * gib)

@@ -23,8 +23,15 @@ def test_buckets():
     assert bucket_of([1024]) == 'single:1024'
     assert bucket_of([1025]) == 'single:2048'
     a, b = bucket_of([64, 128, 9000]), bucket_of([9000, 64, 128])
-    assert a == b and a.startswith('batch:3:')
-    assert bucket_of([64, 128, 9001]) != a
+    assert a == b == 'batch:u4:w26:max16384'
+    # the same make-up shares a key; another make-up does not
+    assert bucket_of([63, 100, 9001]) == a
+    assert bucket_of([64, 128, 8000]) != a
+    assert bucket_of([64, 128, 9000, 9000]) != a
+    # batches drawn from one distribution (other seeds) share their key
+    from gravitation_gb300.scenarios import batch_universes
+    keys = {bucket_of(batch_universes(256, seed)[0]) for seed in (1, 2, 3)}
+    assert len(keys) <= 2, keys
 
 
 def test_store_and_lookup(tmp_path):

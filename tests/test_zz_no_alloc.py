@@ -2,10 +2,13 @@
 device memory where they need forces (code inside another framework's memory pool,
 threads that must not enter the CUDA allocator, hosts that reserve all device memory up
 front).  It keeps its scratch in a fixed device array inside the library, so this test
-checks that two calls in a row -- the second smaller than the first, so that anything
-left over from the first call would show -- give the same accelerations as the regular
-entry points (grav_stage1 + grav_stage2 through the Engine), within the tolerance the
-other tests allow between tile shapes, and that sizes above the limit are refused.
+checks that calls in a row -- the largest size the entry point accepts, then smaller
+ones, so that anything left over from an earlier call would show -- give the same
+accelerations as the regular entry points (grav_stage1 + grav_stage2 through the
+Engine), within the tolerance the other tests allow between tile shapes; that a call
+after the first allocates no device memory (free device memory and the PyTorch
+allocator's counters unchanged across it); that a caller's error flag is left as the
+caller set it; and that sizes above the limit are refused.
 
 The file is named to be collected last; it passes alone in a fresh process (its first
 call does the per-device set-up) and after the other tests.
@@ -25,7 +28,17 @@ from gravitation_gb300.scenarios import G_DEFAULT, uniform_cube
 pytestmark = pytest.mark.gpu
 
 
-def forces_noalloc(r, gm):
+def device_memory_state():
+    """Free device memory (cudaMemGetInfo) and the PyTorch caching allocator's counters."""
+    torch.cuda.synchronize()
+    st = torch.cuda.memory_stats()
+    return (torch.cuda.mem_get_info()[0], st.get('allocated_bytes.all.current', 0),
+            st.get('reserved_bytes.all.current', 0), st.get('num_alloc_retries', 0))
+
+
+def forces_noalloc(r, gm, err_init=0, check_no_alloc=False):
+    """Accelerations through grav_forces_noalloc (every buffer allocated before the
+    call).  With check_no_alloc the device-memory state is compared across the call."""
     L = _lib.load()
     n = len(gm)
     dev = torch.device('cuda', torch.cuda.current_device())
@@ -33,12 +46,16 @@ def forces_noalloc(r, gm):
     rr[:, :3] = torch.as_tensor(r, dtype=torch.float64)
     rr[:, 3] = torch.as_tensor(gm, dtype=torch.float64)
     a = torch.full((n, 4), float('nan'), dtype=torch.float64, device=dev)
-    err = torch.full((1,), -7, dtype=torch.int32, device=dev)
+    err = torch.full((1,), err_init, dtype=torch.int32, device=dev)
     stream = torch.cuda.current_stream(dev)
+    before = device_memory_state() if check_no_alloc else None
     _lib.check(L.grav_forces_noalloc(rr.data_ptr(), a.data_ptr(), n, float(np.max(gm)),
                                      err.data_ptr(), ctypes.c_void_p(stream.cuda_stream)))
     stream.synchronize()
-    assert int(err.item()) == _lib.GRAV_DEV_OK
+    if check_no_alloc:
+        assert device_memory_state() == before
+    # the call never clears the caller's flag: it holds what the caller put there
+    assert int(err.item()) == err_init
     return a[:, :3].cpu().numpy(), a[:, 3].cpu().numpy()
 
 
@@ -51,10 +68,14 @@ def forces_regular(r, gm):
 
 
 def test_noalloc_matches_regular_entry_points_twice(gpu):
-    for n, seed in ((5000, 11), (3001, 12)):
+    sizes = ((_lib.GRAV_NOALLOC_MAX_N, 10), (5000, 11), (3001, 12))
+    for n, seed in sizes:
         r, _, m = uniform_cube(n, seed=seed)
         gm = G_DEFAULT * m
-        a_na, w = forces_noalloc(r, gm)
+        # a repeated call of the same size runs the kernels the first one loaded, so
+        # nothing at all may be allocated by it
+        forces_noalloc(r, gm)
+        a_na, w = forces_noalloc(r, gm, err_init=0, check_no_alloc=True)
         assert np.all(w == 0.0)
         a_reg = forces_regular(r, gm)
         # both FP32 stage 1 with FP64 sums, different tile and grid
@@ -63,6 +84,15 @@ def test_noalloc_matches_regular_entry_points_twice(gpu):
         ref = oracle.accel_fp64(r.astype(np.float32).astype(np.float64), gm32, 1.0,
                                 coincident=True)
         assert oracle.rel_err_per_body(a_na, ref).max() < 1e-5, n
+
+
+def test_noalloc_leaves_the_callers_error_flag(gpu):
+    """A flag the caller already set (say by earlier work sharing it) stays set."""
+    r, _, m = uniform_cube(700, seed=13)
+    gm = G_DEFAULT * m
+    a_na, _ = forces_noalloc(r, gm, err_init=_lib.GRAV_DEV_TIMEOUT)
+    a_reg = forces_regular(r, gm)
+    assert oracle.rel_err_per_body(a_na, a_reg).max() < 2e-6
 
 
 def test_noalloc_refuses_sizes_above_the_limit(gpu):
