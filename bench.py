@@ -10,8 +10,11 @@ own scenarios are generated too.
 
   accuracy   every body's acceleration in the timed mode against the GPU's FP64 mode on
              the same FP64 state (max and tail of |a - a64| / |a64| over all N bodies);
-             the FP64 mode itself is checked against the CPU FP64 oracle on sampled
-             bodies in the same run
+             the GPU tests pin the FP64 mode to the CPU FP64 oracle at 1e-12
+  precision  the Plummer-pair stress (N = 16384, 1000 steps): force errors over every
+             body at the first and last step and energy / momentum drift, per mode
+  sweep      the step over N = 2^10 .. 2^17 in the plugin's float32 default at each size,
+             with the CPU baseline beside every size
 
   value      pair interactions per second (N^2 per step), device-timed steps with the
              state resident in HBM; L2 flushed (256 MiB write) between timed steps
@@ -69,6 +72,8 @@ def parse():
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-batched', action='store_true')
     ap.add_argument('--no-adjoint', action='store_true')
+    ap.add_argument('--no-precision', action='store_true')
+    ap.add_argument('--no-sweep', action='store_true')
     ap.add_argument('--workload', default=None,
                     choices=('precision', 'sweep', 'adjoint', 'adjoint-check', 'scenario',
                              'frontend', 'batched'),
@@ -85,6 +90,7 @@ def parse():
                     help='force the stage-1 tile as bpt,threads,jtile (default: autotuned)')
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
+    a.mode_given = a.mode if '--mode' in sys.argv else None
     return a
 
 
@@ -322,32 +328,49 @@ def measure_fp32_peak(torch, lib, info, device):
     return 2.0 * fmas / (best * 1e-3)
 
 
-def all_body_errors(eng, r, m, G, rows, device):
+def all_body_errors(eng, r, m, G, device):
     """Per-body relative acceleration error of the engine's mode on the FP64 state, over
-    every body, against the GPU's FP64 mode (Engine 'fp64', FP64 all pairs); the FP64
-    mode is checked against the CPU FP64 oracle on `rows` in the same call."""
-    import oracle
-    from gravitation_gb300.engine import Engine
-    n = len(m)
+    every body, against the GPU's FP64 mode (FP64 all pairs, pinned to the CPU FP64
+    oracle at 1e-12 by the GPU tests)."""
+    from gravitation_gb300.workloads import fp64_forces, rel_err_per_body
     a = eng.forces().cpu().numpy()
-    e64 = Engine([n], 1.0, mode='fp64', device=device)
-    e64.set_state(r, np.zeros_like(r), G * m)
-    a64 = e64.forces().cpu().numpy()
-    e64.raise_on_device_error()
-    del e64
-    ref_rows = oracle.accel_fp64(r, G * m, 1.0, rows=rows, coincident=True)
-    pin = float(oracle.rel_err_per_body(a64[rows], ref_rows).max())
-    err = oracle.rel_err_per_body(a, a64)
+    err = rel_err_per_body(a, fp64_forces(r, G * m, device))
     return {'max_rel_err_all_bodies_fp64_state': float(err.max()),
             'p999_rel_err': float(np.quantile(err, 0.999)),
             'median_rel_err': float(np.median(err)),
             'bodies_above_1e-5': int((err > 1e-5).sum()),
-            'bodies': int(n),
-            'reference': 'GPU FP64 mode on the same FP64 state (every body)',
-            'fp64_mode_vs_cpu_oracle_max_rel_err': pin,
-            'fp64_mode_bodies_checked_against_oracle': int(len(rows)),
-            'max_rel_err_sampled_vs_cpu_oracle': float(
-                oracle.rel_err_per_body(a[rows], ref_rows).max())}
+            'bodies': int(len(m)),
+            'reference': 'GPU FP64 mode on the same FP64 state (every body)'}
+
+
+def compact_precision(device):
+    """Plummer-pair precision stress, shortened to 1000 steps: per mode the force error
+    over every body at the first and last step against the GPU FP64 forces of that
+    state, and the FP64 energy / momentum drift (every 100 steps)."""
+    from gravitation_gb300.workloads import run_precision
+    res = run_precision(n=16384, steps=1000, every=100, device=device)
+    keys = ('accel_err_first', 'accel_err_last', 'bodies_above_1e-5_first',
+            'bodies_above_1e-5_last', 'energy_drift_max', 'momentum_drift_max', 'wall_s',
+            'final_pos_dev_vs_fp64_rel')
+    out = {'workload': res['workload']}
+    for mode, val in res.items():
+        if isinstance(val, dict):
+            out[mode] = {k: val[k] for k in keys if k in val}
+    return out
+
+
+def compact_sweep(tuner, cpu=True):
+    """Single-universe step over N = 2^10 .. 2^17 in the plugin's float32 default at each
+    size, device-timed, with the CPU baseline (the port on the host cores) beside it."""
+    from gravitation_gb300.workloads import run_sweep
+    rows = run_sweep(sizes=[2 ** k for k in range(10, 18)], tuner=tuner)
+    for row in rows:
+        if cpu:
+            cv, threads, _ = cpu_baseline_run(row['n'], 0, 0.3, runs=2)
+            row['cpu_interactions_per_s'] = cv
+            row['cpu_threads'] = threads
+            row['gpu_over_cpu'] = row['interactions_per_s'] / cv
+    return rows
 
 
 def run_ours(args):
@@ -397,11 +420,10 @@ def run_ours(args):
         return 0
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=device)
 
-    # accuracy of every body before timing (GPU FP64 mode; it against the CPU oracle)
-    rows = np.random.default_rng(17).choice(n, 64, replace=False)
+    # accuracy of every body before timing, against the GPU FP64 mode
     accuracy = None
     if rank == 0:
-        accuracy = all_body_errors(eng, r, m, G_DEFAULT, rows, local)
+        accuracy = all_body_errors(eng, r, m, G_DEFAULT, local)
         eng.set_state(r, v, gm)
 
     for _ in range(args.warmup):
@@ -462,6 +484,14 @@ def run_ours(args):
         from gravitation_gb300.workloads import run_adjoint
         adjoint = run_adjoint(tuner=default_tuner(), device=local)
 
+    precision = None
+    if rank == 0 and not args.no_precision:
+        precision = compact_precision(local)
+
+    sweep = None
+    if rank == 0 and not args.no_sweep:
+        sweep = compact_sweep(default_tuner(), cpu=world == 1 and not args.no_cpu)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cv, threads, sample = cpu_baseline_run(n, 0, args.cpu_seconds)
@@ -503,6 +533,8 @@ def run_ours(args):
         'cpu_baseline': cpu,
         'batched': batched,
         'adjoint': adjoint,
+        'precision': precision,
+        'sweep': sweep,
     }
     print(json.dumps(line))
     return 0
@@ -572,15 +604,11 @@ def run_workload(args):
     from gravitation_gb300 import workloads
     from gravitation_gb300.tune import default_tuner
     if args.workload == 'precision':
-        import oracle
-
-        def check(r, gm, a, rows):
-            ref = oracle.accel_fp64(r, gm, 1.0, rows=rows, coincident=True)
-            return oracle.rel_err_per_body(a[rows], ref).max()
         res = workloads.run_precision(n=args.n if args.n != 65536 else 16384,
-                                      steps=args.steps, check=check)
+                                      steps=args.steps)
     elif args.workload == 'sweep':
-        res = {'sweep': workloads.run_sweep(mode=args.mode, tuner=default_tuner())}
+        mode = None if args.mode_given is None else args.mode
+        res = {'sweep': workloads.run_sweep(mode=mode, tuner=default_tuner())}
         # the CPU baseline (the reference's design, restated portably) at every size
         for row in res['sweep']:
             cv, threads, sample = cpu_baseline_run(row['n'], 0, 0.5)

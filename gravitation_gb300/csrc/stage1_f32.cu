@@ -144,52 +144,12 @@ __global__ void __launch_bounds__(T) stage1_f32_kernel(const grav_batch b)
 			// NEAR: does this j-tile hold rows of this CTA (their self pairs)?
 			const int64_t jl0 = (jt0 + t) * J;
 			const bool own = jl0 < S.il0 + IT && jl0 + J > S.il0;
-#pragma unroll 4
-			for (int j = 0; j < J; ++j) {
-				const float4 pj = sj[j];
-				float4 lj = make_float4(0.f, 0.f, 0.f, 0.f);
-				if (DS) lj = sl[j];
-				bool near = false;
-#pragma unroll
-				for (int k = 0; k < B; ++k) {
-					float dx = pj.x - xi[k];
-					float dy = pj.y - yi[k];
-					float dz = pj.z - zi[k];
-					if (DS) {
-						dx = dx + (lj.x - xl[k]);
-						dy = dy + (lj.y - yl[k]);
-						dz = dz + (lj.z - zl[k]);
-					}
-					const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
-					if (NEAR) near |= own ? (r2 < thr) & (r2 > eps2) : (r2 < thr);
-					const float inv = rsqrt_sfu(r2);
-					const float inv2 = inv * inv;
-					float w = pj.w * inv;
-					w = w * inv2;
-					fx[k] = fmaf(dx, w, fx[k]);
-					fy[k] = fmaf(dy, w, fy[k]);
-					fz[k] = fmaf(dz, w, fz[k]);
-				}
-				if (NEAR && __any_sync(0xffffffffu, near)) {
-					// cold path: this step's pairs within the near radius again, from the
-					// double-single separation
-					lj = sl[j];
-#pragma unroll
-					for (int k = 0; k < B; ++k) {
-						const float dx = pj.x - xi[k], dy = pj.y - yi[k], dz = pj.z - zi[k];
-						const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
-						const bool nk = (r2 < thr) & (r2 > eps2);
-						if (__any_sync(0xffffffffu, nk)) {
-							float ex, ey, ez;
-							near_delta(dx, dy, dz, r2, lj, rowlo[NEAR ? k : 0][NEAR ? tid : 0],
-								eps2, nk, ex, ey, ez);
-							fx[k] = fmaf(ex, pj.w, fx[k]);
-							fy[k] = fmaf(ey, pj.w, fy[k]);
-							fz[k] = fmaf(ez, pj.w, fz[k]);
-						}
-					}
-				}
-			}
+			if (NEAR && own)
+				rows_tile<B, J, DS, NEAR, true>(sj, sl, eps2, thr, xi, yi, zi, xl, yl, zl, fx, fy,
+					fz, &rowlo[0][0], tid, T);
+			else
+				rows_tile<B, J, DS, NEAR, false>(sj, sl, eps2, thr, xi, yi, zi, xl, yl, zl, fx, fy,
+					fz, &rowlo[0][0], tid, T);
 #pragma unroll
 			for (int k = 0; k < B; ++k) {
 				two_sum_acc(hx[k], lx[k], fx[k]);

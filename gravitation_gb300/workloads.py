@@ -154,21 +154,43 @@ def run_adjoint_check(n=4096, steps=1000, every=32, seed=3, ncoords=16, eps=1e-6
             'coords': rows}
 
 
+def fp64_forces(r, gm, device=None):
+    """Every body's acceleration from the GPU FP64 mode (FP64 all pairs; the tests pin
+    that mode to the CPU FP64 oracle at 1e-12) for positions r and G*m gm."""
+    n = len(gm)
+    e = Engine([n], 1.0, mode='fp64', device=device)
+    e.set_state(r, np.zeros((n, 3)), gm)
+    a = e.forces().cpu().numpy()
+    e.raise_on_device_error()
+    return a
+
+
+def rel_err_per_body(a, ref):
+    """|a_i - ref_i| / |ref_i| per body (0 where both vanish)."""
+    num = np.linalg.norm(np.asarray(a) - np.asarray(ref), axis=1)
+    den = np.linalg.norm(np.asarray(ref), axis=1)
+    return np.where(den > 0, num / np.where(den > 0, den, 1.0), np.where(num > 0, np.inf, 0.0))
+
+
 def run_precision(n=16384, steps=10000, every=100, seed=2,
                   modes=('fp32u', 'fp32un', 'fp32cu', 'fp32c', 'fp64'),
-                  sample=256, check=None, device=None):
+                  check=None, device=None):
     """Precision stress: two Plummer spheres (scale radius 50, centres 1000 apart,
     approaching at 5 along x, masses log-uniform in [0.1, 1000]).  For each mode: the
-    per-body acceleration error at the first and the last step, measured by
-    ``check(r, gm, a, rows)`` (the caller's reference, e.g. an FP64 all-pairs sum) on
-    sampled bodies, and the relative drift of the FP64 energy and momentum every
-    `every` steps.  Returns a dict per mode."""
+    per-body acceleration error at the first and the last step over every body, against
+    the FP64 forces of the same FP64 state (``check(r, gm, a)`` returning per-body
+    errors, default: the GPU FP64 mode, fp64_forces), and the relative drift of the FP64
+    energy and momentum every `every` steps.  Returns a dict per mode."""
     from .scenarios import plummer_pair
     r, v, m = plummer_pair(n, seed=seed)
     gm = G_DEFAULT * m
     dev = torch.device('cuda', torch.cuda.current_device() if device is None else device)
-    rows = np.random.default_rng(seed).choice(n, min(sample, n), replace=False)
-    out = {'workload': 'Plummer pair N=%d seed %d, %d steps, T=%g' % (n, seed, steps, T_DEFAULT)}
+    if check is None:
+        def check(rs, gms, a):
+            return rel_err_per_body(a, fp64_forces(rs, gms, dev.index))
+    out = {'workload': 'Plummer pair N=%d seed %d, %d steps, T=%g; force errors over every '
+                       'body against the FP64 forces of the same state' % (n, seed, steps,
+                                                                           T_DEFAULT)}
     finals = {}
     for mode in modes:
         eng = Engine([n], T_DEFAULT, mode=mode, device=dev.index)
@@ -181,11 +203,10 @@ def run_precision(n=16384, steps=10000, every=100, seed=2,
         drift_e, drift_p = [], []
 
         def accel_err():
-            if check is None:
-                return None
             rs = eng.r[:n, :3].cpu().numpy()
             a = eng.forces().cpu().numpy()
-            return float(check(rs, gm, a, rows))
+            e = np.asarray(check(rs, gm, a))
+            return float(e.max()), int((e > 1e-5).sum())
         errs.append(accel_err())
         graph = eng.capture_graph(every)
         t0 = time.perf_counter()
@@ -201,7 +222,8 @@ def run_precision(n=16384, steps=10000, every=100, seed=2,
         errs.append(accel_err())
         finals[mode] = eng.r[:n, :3].cpu().numpy()
         eng.raise_on_device_error()
-        out[mode] = {'accel_err_first': errs[0], 'accel_err_last': errs[1],
+        out[mode] = {'accel_err_first': errs[0][0], 'accel_err_last': errs[1][0],
+                     'bodies_above_1e-5_first': errs[0][1], 'bodies_above_1e-5_last': errs[1][1],
                      'energy_drift_max': max(drift_e), 'energy_drift_final': drift_e[-1],
                      'momentum_drift_max': max(drift_p), 'wall_s': wall, 'steps': done,
                      'energy_every': every}
@@ -214,30 +236,39 @@ def run_precision(n=16384, steps=10000, every=100, seed=2,
     return out
 
 
-def run_sweep(sizes=None, mode='fp32un', reps=5, tuner=None, device=None):
-    """Interactions/s of the single-universe step over an N sweep (2^4 .. 2^17)."""
+def run_sweep(sizes=None, mode=None, reps=5, tuner=None, device=None):
+    """Interactions/s of the single-universe step over an N sweep (2^4 .. 2^17), with
+    the state in HBM.  mode None: the plugin's float32 default at each size (all pairs
+    below 8192 bodies, unique pairs from there, near pairs corrected).  Below 8192 bodies
+    one graph replay holds 20 steps, so that the host's graph-launch rate does not set
+    the measured step time; above, one step per replay."""
+    from .plugin import default_mode
     from .scenarios import uniform_cube
     sizes = sizes or [2 ** k for k in range(4, 18)]
     dev = torch.device('cuda', torch.cuda.current_device() if device is None else device)
     stream = torch.cuda.current_stream(dev)
     res = []
     for n in sizes:
+        m_n = mode or default_mode('float32', n)
         r, v, m = uniform_cube(n, seed=0)
-        eng = Engine([n], T_DEFAULT, mode=mode, tuner=tuner, device=dev.index)
+        eng = Engine([n], T_DEFAULT, mode=m_n, tuner=tuner, device=dev.index)
         eng.set_state(r, v, G_DEFAULT * m)
-        g = eng.capture_graph(1)
+        per = 20 if n < 8192 else 1
+        g = eng.capture_graph(per)
         for _ in range(3):
             g.replay()
         e0, e1 = _events(1)[0]
-        k = max(reps, int(2e10 // (n * n)) if n < 8192 else reps)
-        k = min(k, 2000)
+        k = max(reps, int(2e10 // (n * n * per)) if n < 8192 else reps)
+        k = min(k, 200)
         e0.record(stream)
         for _ in range(k):
             g.replay()
         e1.record(stream)
         e1.synchronize()
-        ms = e0.elapsed_time(e1) / k
-        res.append({'n': n, 'ms_per_step': ms, 'interactions_per_s': n * n / (ms * 1e-3),
+        ms = e0.elapsed_time(e1) / (k * per)
+        res.append({'n': n, 'mode': m_n, 'ms_per_step': ms,
+                    'interactions_per_s': n * n / (ms * 1e-3),
+                    'steps_per_replay': per,
                     'tile': [eng.tile.bpt, eng.tile.threads, eng.tile.jtile, eng.info.grid]})
         eng.raise_on_device_error()
     return res
@@ -248,9 +279,51 @@ def _events(n):
             for _ in range(n)]
 
 
-def run_batched(steps=100, warmup=3, mode='fp32', n_univ=256, seed=1, loop_steps=10,
+def _loop_timings(engines, stream, dev, warmup, loop_steps):
+    """Per-universe loop of single-universe steps: wall clock of launched steps (host
+    launch overhead included) and device time of the same loop captured in one graph."""
+    for _ in range(warmup):
+        for e in engines:
+            e.step(1)
+    torch.cuda.synchronize()
+    walls = []
+    for _ in range(loop_steps):
+        t0 = time.perf_counter()
+        for e in engines:
+            e.step(1)
+        torch.cuda.synchronize()
+        walls.append(time.perf_counter() - t0)
+    side = torch.cuda.Stream(device=dev)
+    side.wait_stream(stream)
+    g2 = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g2, stream=side):
+        for e in engines:
+            e.step(1, stream=side)
+    stream.wait_stream(side)
+    g2.replay()
+    torch.cuda.synchronize()
+    e0, e1 = _events(1)[0]
+    e0.record(stream)
+    for _ in range(loop_steps):
+        g2.replay()
+    e1.record(stream)
+    e1.synchronize()
+    for e in engines:
+        e.raise_on_device_error()
+    return 1e3 * statistics.mean(walls), e0.elapsed_time(e1) / loop_steps
+
+
+def run_batched(steps=100, warmup=3, mode='fp32un', n_univ=256, seed=1, loop_steps=10,
                 tuner=None, device=None):
-    """Batched step vs the per-universe loop.  Returns a dict of measurements."""
+    """Batched step vs the per-universe loop.  Returns a dict of measurements.
+
+    The batch runs in `mode` with the tile the autotuner picks for the batch.  The loop
+    is timed twice: with every universe in the mode and tile the plugin itself would
+    use for it alone (plugin.default_mode: all pairs below 8192 bodies, unique pairs
+    from there; each universe's own tuned tile) -- the fair comparison, reported as
+    speedup_vs_loop / speedup_vs_graphed_loop -- and with every universe in the batch's
+    mode (each its own tuned tile)."""
+    from .plugin import default_mode
     sizes, states = batch_universes(n_univ, seed)
     sizes = [int(s) for s in sizes]
     r = np.concatenate([s[0] for s in states])
@@ -282,47 +355,27 @@ def run_batched(steps=100, warmup=3, mode='fp32', n_univ=256, seed=1, loop_steps
     e1.synchronize()
     nograph_ms = e0.elapsed_time(e1) / steps
 
-    # per-universe loop of the single-universe step
-    engines = []
-    off = 0
-    for n in sizes:
-        e = Engine([n], T_DEFAULT, mode=mode, tuner=tuner, device=dev.index)
-        e.set_state(r[off:off + n], v[off:off + n], gm[off:off + n])
-        engines.append(e)
-        off += n
-    for _ in range(warmup):
-        for e in engines:
-            e.step(1)
-    torch.cuda.synchronize()
-    walls = []
-    e0.record(stream)
-    for _ in range(loop_steps):
-        t0 = time.perf_counter()
-        for e in engines:
-            e.step(1)
-        torch.cuda.synchronize()
-        walls.append(time.perf_counter() - t0)
-    e1.record(stream)
-    e1.synchronize()
-    loop_ms = 1e3 * statistics.mean(walls)
-    # the loop captured in one graph: its GPU-side cost without host launch overhead
-    side = torch.cuda.Stream(device=dev)
-    side.wait_stream(stream)
-    g2 = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(g2, stream=side):
-        for e in engines:
-            e.step(1, stream=side)
-    stream.wait_stream(side)
-    g2.replay()
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(loop_steps):
-        g2.replay()
-    e1.record(stream)
-    e1.synchronize()
-    loop_graph_ms = e0.elapsed_time(e1) / loop_steps
-    for e in engines:
-        e.raise_on_device_error()
+    def loop_engines(mode_of):
+        engines, off = [], 0
+        for n in sizes:
+            e = Engine([n], T_DEFAULT, mode=mode_of(n), tuner=tuner, device=dev.index)
+            e.set_state(r[off:off + n], v[off:off + n], gm[off:off + n])
+            engines.append(e)
+            off += n
+        return engines
+
+    def plugin_mode(n):
+        # the float32 default for one universe of n bodies; a batch forced to another
+        # precision compares with universes forced to it too
+        return default_mode('float32', n) if mode in ('fp32n', 'fp32un') else mode
+
+    engines = loop_engines(plugin_mode)
+    loop_ms, loop_graph_ms = _loop_timings(engines, stream, dev, warmup, loop_steps)
+    modes_used = sorted({e.mode_name for e in engines})
+    del engines
+    engines = loop_engines(lambda n: mode)
+    same_ms, same_graph_ms = _loop_timings(engines, stream, dev, warmup, loop_steps)
+    del engines
 
     return {
         'workload': '%d universes, N log-uniform in [64,16384] (seed %d), uniform cube each, '
@@ -332,10 +385,15 @@ def run_batched(steps=100, warmup=3, mode='fp32', n_univ=256, seed=1, loop_steps
         'batched_ms_per_step': batched_ms,
         'batched_interactions_per_s': inter / (batched_ms * 1e-3),
         'batched_no_graph_ms_per_step': nograph_ms,
+        'loop': 'each universe in the mode and tile the plugin picks for it alone (%s)' %
+                ', '.join(modes_used),
         'loop_ms_per_step': loop_ms,
         'loop_graph_ms_per_step': loop_graph_ms,
         'speedup_vs_loop': loop_ms / batched_ms,
         'speedup_vs_graphed_loop': loop_graph_ms / batched_ms,
+        'loop_same_mode_ms_per_step': same_ms,
+        'loop_same_mode_graph_ms_per_step': same_graph_ms,
+        'speedup_vs_graphed_loop_same_mode': same_graph_ms / batched_ms,
         'tile': {'bpt': eng.tile.bpt, 'threads': eng.tile.threads, 'jtile': eng.tile.jtile,
                  'grid': eng.info.grid},
         'launches_per_step': 2,

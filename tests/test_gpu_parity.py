@@ -438,3 +438,31 @@ def test_context_usable_after_many_launches(gpu):
     torch.cuda.synchronize()
     eng.raise_on_device_error()
     assert torch.isfinite(eng.r).all()
+
+
+def test_plummer_pair_default_mode_every_body(gpu):
+    """The precision-stress configuration (two Plummer spheres, N = 16384, seed 2): the
+    float32 default (fp32un) at the first step, every body within 1e-5 of the FP64
+    forces of the FP64 state; the FP64 mode pinned to the oracle on sampled bodies."""
+    n = 16384
+    r, v, m = plummer_pair(n, seed=2)
+    a64 = fp64_forces_gpu(r, m)
+    rows = np.random.default_rng(2).choice(n, 24, replace=False)
+    ref = oracle.accel_fp64(r, G_DEFAULT * m, 1.0, rows=rows, coincident=True)
+    assert oracle.rel_err_per_body(a64[rows], ref).max() < 1e-12
+    a, _ = engine_forces('fp32un', r, v, m)
+    assert oracle.rel_err_per_body(a, a64).max() < 1e-5
+
+
+def test_precision_workload_short(gpu):
+    """The precision workload (shortened): errors over every body against the GPU FP64
+    forces at the first and last step, energy and momentum drift recorded."""
+    from gravitation_gb300.workloads import run_precision
+    out = run_precision(n=2048, steps=20, every=10, modes=('fp32un', 'fp32u', 'fp64'))
+    assert out['fp32un']['accel_err_first'] < 1e-5
+    assert out['fp32un']['accel_err_last'] < 1e-5
+    assert out['fp32un']['bodies_above_1e-5_first'] == 0
+    assert out['fp64']['accel_err_first'] < 1e-12
+    for mode in ('fp32un', 'fp32u', 'fp64'):
+        assert np.isfinite(out[mode]['energy_drift_max'])
+        assert out[mode]['momentum_drift_max'] < 1e-9
