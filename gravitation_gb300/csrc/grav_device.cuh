@@ -185,11 +185,13 @@ __device__ __forceinline__ void near_delta(float dx, float dy, float dz, float r
 }
 
 // One j-tile against a thread's B rows, every ordered pair, rows only: the inner loop
-// of the all-pairs kernel (stage1_f32.cu) and of the unique-pair kernel's diagonal
-// blocks (stage1_sym.cu); the rows' low parts are rowlo[k * T + tid].  NEAR adds the near
+// of the all-pairs kernel (stage1_f32.cu); the rows' low parts are rowlo[k * T + tid].
+// (The unique-pair kernel keeps its own copy of this loop with a test per step: with
+// this function inlined there its main loop compiled measurably slower on GB300.)  NEAR adds the near
 // test (one three-input min per two rows and a compare; with SELF -- tiles that hold the
 // thread block's own rows -- a test per pair that also excludes r2 = eps2, so that self
-// pairs do not send the warp down the correction path) and the cold correction path.
+// pairs do not count) whose result is a bit per step, and after every 32 steps a cold
+// path over the steps where some lane of the warp met a near pair.
 template <int B, int JT, bool DS, bool NEAR, bool SELF>
 __device__ __forceinline__ void rows_tile(const float4* __restrict__ sj,
 	const float4* __restrict__ sjl, float eps2, float thr, const float (&xi)[B],
@@ -197,45 +199,57 @@ __device__ __forceinline__ void rows_tile(const float4* __restrict__ sj,
 	const float (&zl)[B], float (&fx)[B], float (&fy)[B], float (&fz)[B],
 	const float4* __restrict__ rowlo, int tid, int T)
 {
+	static_assert(JT % 32 == 0, "j-tiles of whole 32-body groups");
+#pragma unroll 1
+	for (int j0 = 0; j0 < JT; j0 += 32) {
+		uint32_t nmask = 0;
 #pragma unroll 4
-	for (int j = 0; j < JT; ++j) {
-		const float4 pj = sj[j];
-		float4 lj = make_float4(0.f, 0.f, 0.f, 0.f);
-		if (DS) lj = sjl[j];
-		float rmin = 0.f, rprev = 0.f;
-		bool near = false;
-#pragma unroll
-		for (int k = 0; k < B; ++k) {
-			float dx = pj.x - xi[k], dy = pj.y - yi[k], dz = pj.z - zi[k];
-			if (DS) {
-				dx = dx + (lj.x - xl[k]);
-				dy = dy + (lj.y - yl[k]);
-				dz = dz + (lj.z - zl[k]);
-			}
-			const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
-			if (NEAR && SELF) near |= (r2 < thr) & (r2 > eps2);
-			if (NEAR && !SELF) near_min_step<B>(k, r2, rmin, rprev);
-			const float inv = rsqrt_sfu(r2);
-			float w = pj.w * inv;
-			w = w * (inv * inv);
-			fx[k] = fmaf(dx, w, fx[k]);
-			fy[k] = fmaf(dy, w, fy[k]);
-			fz[k] = fmaf(dz, w, fz[k]);
-		}
-		if (NEAR && !SELF) near = rmin < thr;
-		if (NEAR && __any_sync(0xffffffffu, near)) {
-			lj = sjl[j];
+		for (int jj = 0; jj < 32; ++jj) {
+			const float4 pj = sj[j0 + jj];
+			float4 lj = make_float4(0.f, 0.f, 0.f, 0.f);
+			if (DS) lj = sjl[j0 + jj];
+			float rmin = 0.f, rprev = 0.f;
+			bool near = false;
 #pragma unroll
 			for (int k = 0; k < B; ++k) {
-				const float dx = pj.x - xi[k], dy = pj.y - yi[k], dz = pj.z - zi[k];
+				float dx = pj.x - xi[k], dy = pj.y - yi[k], dz = pj.z - zi[k];
+				if (DS) {
+					dx = dx + (lj.x - xl[k]);
+					dy = dy + (lj.y - yl[k]);
+					dz = dz + (lj.z - zl[k]);
+				}
 				const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
-				const bool nk = (r2 < thr) & (r2 > eps2);
-				if (__any_sync(0xffffffffu, nk)) {
-					float ex, ey, ez;
-					near_delta(dx, dy, dz, r2, lj, rowlo[k * T + tid], eps2, nk, ex, ey, ez);
-					fx[k] = fmaf(ex, pj.w, fx[k]);
-					fy[k] = fmaf(ey, pj.w, fy[k]);
-					fz[k] = fmaf(ez, pj.w, fz[k]);
+				if (NEAR && SELF) near |= (r2 < thr) & (r2 > eps2);
+				if (NEAR && !SELF) near_min_step<B>(k, r2, rmin, rprev);
+				const float inv = rsqrt_sfu(r2);
+				float w = pj.w * inv;
+				w = w * (inv * inv);
+				fx[k] = fmaf(dx, w, fx[k]);
+				fy[k] = fmaf(dy, w, fy[k]);
+				fz[k] = fmaf(dz, w, fz[k]);
+			}
+			if (NEAR && !SELF) near = rmin < thr;
+			if (NEAR && near) nmask |= 1u << jj;
+		}
+		if (NEAR) {
+			uint32_t todo = __reduce_or_sync(0xffffffffu, nmask);
+			while (todo) {
+				const int jj = __ffs(todo) - 1;
+				todo &= todo - 1;
+				const float4 pj = sj[j0 + jj];
+				const float4 lj = sjl[j0 + jj];
+#pragma unroll
+				for (int k = 0; k < B; ++k) {
+					const float dx = pj.x - xi[k], dy = pj.y - yi[k], dz = pj.z - zi[k];
+					const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+					const bool nk = (r2 < thr) & (r2 > eps2);
+					if (__any_sync(0xffffffffu, nk)) {
+						float ex, ey, ez;
+						near_delta(dx, dy, dz, r2, lj, rowlo[k * T + tid], eps2, nk, ex, ey, ez);
+						fx[k] = fmaf(ex, pj.w, fx[k]);
+						fy[k] = fmaf(ey, pj.w, fy[k]);
+						fz[k] = fmaf(ez, pj.w, fz[k]);
+					}
 				}
 			}
 		}

@@ -184,16 +184,53 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 			const float4* __restrict__ sjl = sj + JT;  // low parts (NP == 2)
 			const int blkJ = static_cast<int>(jt / TPB);
 			if (blkJ == blkI) {
-				// diagonal block: every ordered pair of the block once, rows only; a tile
-				// holding this warp's own rows meets their self pairs
+				// diagonal block: every ordered pair of the block once, rows only.  In NEAR
+				// mode a tile that holds this warp's own rows meets their self pairs (d = 0,
+				// r2 = eps2): there the near test also requires r2 > eps2, so that self pairs
+				// do not send the warp down the correction path
 				const int jl0 = static_cast<int>(jt - static_cast<int64_t>(blkI) * TPB) * JT;
 				const bool own = jl0 < (warp + 1) * 32 * B && jl0 + JT > warp * 32 * B;
-				if (NEAR && own)
-					rows_tile<B, JT, DS, NEAR, true>(sj, sjl, eps2, thr, xi, yi, zi, xl, yl, zl,
-						fx, fy, fz, &rowlo[0][0], tid, T);
-				else
-					rows_tile<B, JT, DS, NEAR, false>(sj, sjl, eps2, thr, xi, yi, zi, xl, yl, zl,
-						fx, fy, fz, &rowlo[0][0], tid, T);
+#pragma unroll 4
+				for (int j = 0; j < JT; ++j) {
+					const float4 pj = sj[j];
+					float4 lj = make_float4(0.f, 0.f, 0.f, 0.f);
+					if (DS) lj = sjl[j];
+					bool near = false;
+#pragma unroll
+					for (int k = 0; k < B; ++k) {
+						float dx = pj.x - xi[k], dy = pj.y - yi[k], dz = pj.z - zi[k];
+						if (DS) {
+							dx = dx + (lj.x - xl[k]);
+							dy = dy + (lj.y - yl[k]);
+							dz = dz + (lj.z - zl[k]);
+						}
+						const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+						if (NEAR) near |= own ? (r2 < thr) & (r2 > eps2) : (r2 < thr);
+						const float inv = rsqrt_sfu(r2);
+						float w = pj.w * inv;
+						w = w * (inv * inv);
+						fx[k] = fmaf(dx, w, fx[k]);
+						fy[k] = fmaf(dy, w, fy[k]);
+						fz[k] = fmaf(dz, w, fz[k]);
+					}
+					if (NEAR && __any_sync(0xffffffffu, near)) {
+						lj = sjl[j];
+#pragma unroll
+						for (int k = 0; k < B; ++k) {
+							const float dx = pj.x - xi[k], dy = pj.y - yi[k], dz = pj.z - zi[k];
+							const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+							const bool nk = (r2 < thr) & (r2 > eps2);
+							if (__any_sync(0xffffffffu, nk)) {
+								float ex, ey, ez;
+								near_delta(dx, dy, dz, r2, lj, rowlo[NEAR ? k : 0][NEAR ? tid : 0],
+									eps2, nk, ex, ey, ez);
+								fx[k] = fmaf(ex, pj.w, fx[k]);
+								fy[k] = fmaf(ey, pj.w, fy[k]);
+								fz[k] = fmaf(ez, pj.w, fz[k]);
+							}
+						}
+					}
+				}
 			} else {
 				// unique pairs with block J > I: rotate the chunk's column sums
 #pragma unroll 1
