@@ -169,12 +169,18 @@ class Rollout:
         self.every = max(1, int(every))
         if mode is None:
             # the forward's FP32 kernel by size, as the plugin picks it: all pairs for
-            # small universes, unique pairs from 8192 bodies while the batch's slots fit
+            # small universes, unique pairs from 8192 bodies while the batch's slots fit,
+            # near pairs from double-single separations.  A final-state loss against a
+            # nearby target is ill-conditioned (at the differentiable-rollout workload
+            # r_K - t is ~1e-9 of r_K), so the forward's force error reaches the
+            # gradients through dL/dr_K: plain FP32 separations put them ~1e-3 off the
+            # exact FP64 gradients there, the near-corrected ones ~7e-5
             from .plugin import UNIQUE_PAIRS_FROM_N
             from .engine import pair_plan_fits
-            mode = 'fp32'
-            if max(self.sizes, default=0) >= UNIQUE_PAIRS_FROM_N and pair_plan_fits(self.sizes):
-                mode = 'fp32u'
+            mode = 'fp32n'
+            if max(self.sizes, default=0) >= UNIQUE_PAIRS_FROM_N and pair_plan_fits(
+                    self.sizes, mode='fp32un'):
+                mode = 'fp32un'
         self.fwd = Engine(self.sizes, self.T, mode=mode, tile=fwd_tile, device=device,
                           tuner=tuner)
         self.adj = AdjointEngine(self.sizes, self.T, device=device, pairs=adj_pairs)
@@ -333,3 +339,31 @@ def torch_reference_rollout(r0, v0, m, G, T, steps):
         v = v + T * a
         r = r + T * v
     return r, v
+
+
+def reference_gradients_fp64(r0, v0, m, G, T, steps, g_rK, g_vK, every=8):
+    """Gradients (dL/dr0, dL/dv0, dL/dm) of a final-state loss with incoming gradients
+    g_rK, g_vK, by autograd through the plain PyTorch FP64 integrator
+    (torch_reference_rollout) with checkpoints every ``every`` steps: the forward keeps
+    only the segment starts, and each segment is replayed with autograd in reverse
+    order, so device memory stays at a few N x N x 3 FP64 tensors per step of one
+    segment.  A reference for the adjoint kernels, not a fast path."""
+    r, v = r0.detach(), v0.detach()
+    m = m.detach()
+    starts = list(range(0, steps, every))
+    ckpt = []
+    with torch.no_grad():
+        for s0 in starts:
+            ckpt.append((r, v))
+            r, v = torch_reference_rollout(r, v, m, G, T, min(every, steps - s0))
+    gr, gv = g_rK.detach(), g_vK.detach()
+    gm = torch.zeros_like(m)
+    for s0, (rc, vc) in zip(reversed(starts), reversed(ckpt)):
+        rs = rc.clone().requires_grad_(True)
+        vs = vc.clone().requires_grad_(True)
+        ms = m.clone().requires_grad_(True)
+        re, ve = torch_reference_rollout(rs, vs, ms, G, T, min(every, steps - s0))
+        gr, gv, gms = torch.autograd.grad((re, ve), (rs, vs, ms), (gr, gv))
+        gm = gm + gms
+        del re, ve
+    return gr, gv, gm

@@ -83,12 +83,15 @@ def run_adjoint(n=4096, steps=1000, every=32, seed=3, reps=3, tuner=None, device
 
 
 def run_adjoint_check(n=4096, steps=1000, every=32, seed=3, ncoords=16, eps=1e-6,
-                      device=None):
+                      device=None, reference=True):
     """Gradients of the differentiable-rollout workload (N=4096, 1000 steps, checkpoint
     every 32) against FP64 central finite differences with step eps on `ncoords` seeded
     coordinates of (r0, v0, m).  The finite differences run full FP64 rollouts on the
     GPU (fp64 mode); the target is the same FP64 run with masses scaled by the seeded
-    factor in [0.99, 1.01].  Returns per-coordinate gradients and relative errors."""
+    factor in [0.99, 1.01].  Returns per-coordinate gradients and relative errors, and
+    (reference=True) every body's gradients against the exact FP64 discrete gradients
+    (adjoint_reference_errors), which also resolve the mass gradients that finite
+    differences cannot at this configuration."""
     from .adjoint import Rollout
     from .scenarios import mass_perturbation, uniform_cube
     r, v, m = uniform_cube(n, seed=seed)
@@ -146,12 +149,52 @@ def run_adjoint_check(n=4096, steps=1000, every=32, seed=3, ncoords=16, eps=1e-6
                      'fd': fd, 'rel_err': abs(g - fd) / max(abs(fd), 1e-300)})
     e64.raise_on_device_error()
     errs = {k: [x['rel_err'] for x in rows if x['var'] == k] for k in ('r0', 'v0', 'm')}
-    return {'workload': 'N=%d uniform cube seed %d, %d steps, checkpoint every %d; FD eps %g '
-                        'on %d seeded coordinates' % (n, seed, steps, every, eps, ncoords),
-            'loss_fp64': loss(r, v, m), 'loss_adjoint_forward': loss_adj,
-            'max_rel_err': {k: (max(vs) if vs else None) for k, vs in errs.items()},
-            'median_rel_err': {k: (float(np.median(vs)) if vs else None) for k, vs in errs.items()},
-            'coords': rows}
+    out = {'workload': 'N=%d uniform cube seed %d, %d steps, checkpoint every %d; FD eps %g '
+                       'on %d seeded coordinates' % (n, seed, steps, every, eps, ncoords),
+           'loss_fp64': loss(r, v, m), 'loss_adjoint_forward': loss_adj,
+           'max_rel_err': {k: (max(vs) if vs else None) for k, vs in errs.items()},
+           'median_rel_err': {k: (float(np.median(vs)) if vs else None) for k, vs in errs.items()},
+           'coords': rows}
+    if reference:
+        out['fp64_reference'] = adjoint_reference_errors(
+            r, v, m, tt, steps, (g_r, g_v, g_m), rows, dev)
+    return out
+
+
+def adjoint_reference_errors(r, v, m, target, steps, grads, coords, dev, every=8):
+    """The adjoint's gradients (FP32 pair terms, FP64 state) against the exact FP64
+    discrete gradients of the same loss, by autograd through the plain PyTorch FP64
+    integrator with checkpoints (adjoint.reference_gradients_fp64), over every body:
+    ||g - g64|| / ||g64|| for r0, v0 and m, the largest per-body error relative to the
+    largest per-body gradient, and the finite differences' own error on `coords`."""
+    from .adjoint import reference_gradients_fp64, torch_reference_rollout
+    n = len(m)
+    t0 = time.perf_counter()
+    r0 = torch.tensor(r, device=dev)
+    v0 = torch.tensor(v, device=dev)
+    mm = torch.tensor(m, device=dev)
+    with torch.no_grad():
+        rk64, _ = torch_reference_rollout(r0, v0, mm, G_DEFAULT, T_DEFAULT, steps)
+    g_rK = (2.0 / n) * (rk64 - target)
+    ref = reference_gradients_fp64(r0, v0, mm, G_DEFAULT, T_DEFAULT, steps, g_rK,
+                                   torch.zeros_like(g_rK), every=every)
+    ref = [x.cpu().numpy() for x in ref]
+    res = {'reference': 'autograd through a plain PyTorch FP64 integrator (checkpoints '
+                        'every %d steps), same loss, every body' % every,
+           'seconds': time.perf_counter() - t0}
+    for name, g, g64 in zip(('r0', 'v0', 'm'), grads, ref):
+        g = np.asarray(g).reshape(g64.shape)
+        diff = np.abs(g - g64).reshape(n, -1).max(1)
+        res[name] = {'rel_err_norm': float(np.linalg.norm(g - g64) / np.linalg.norm(g64)),
+                     'max_body_err_over_max_grad': float(diff.max() / np.abs(g64).max())}
+    fd_err = {'r0': [], 'v0': [], 'm': []}
+    for c in coords:
+        g64 = ref[('r0', 'v0', 'm').index(c['var'])]
+        val = g64[c['body']] if c['var'] == 'm' else g64[c['body'], c['comp']]
+        c['fp64_reference'] = float(val)
+        fd_err[c['var']].append(abs(c['fd'] - val) / max(abs(val), 1e-300))
+    res['fd_rel_err_vs_reference_max'] = {k: (max(x) if x else None) for k, x in fd_err.items()}
+    return res
 
 
 def fp64_forces(r, gm, device=None):

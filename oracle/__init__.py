@@ -18,6 +18,8 @@ Contents
   rollout_fp64        stage 1 (FP64) + stage 2 (FP64) for k steps
   energy_fp64         kinetic, potential and momentum in FP64
   vjp_fp64            discrete adjoint of one stage 1 (J_A^T u and dA/dm terms)
+  adjoint_rollout_fp64  discrete adjoint of a checkpointed FP64 rollout (gradients of a
+                      final-state loss with respect to r0, v0 and m)
   port_stage1         portable restatement of the reference's fastest CPU kernel
                       design (c4a/cy4), FP32, OpenMP -- the CPU baseline
 """
@@ -267,6 +269,40 @@ def vjp_fp64(r, m, G, u, threads=None):
     lib().orc_vjp_fp64(_ptr(r, _dp), _ptr(m, _dp), float(G), _ptr(u, _dp), n,
                        _ptr(h, _dp), _ptr(g, _dp), int(threads or default_threads()))
     return h, g
+
+
+def adjoint_rollout_fp64(r0, v0, m, G, T, steps, g_rK, g_vK, every=32, threads=None):
+    """Discrete adjoint of ``steps`` FP64 symplectic-Euler steps (stage 1 all pairs,
+    stage 2 of _base_.py:58-62), reverse sweep with checkpoints every ``every`` steps
+    and the states of a segment recomputed from its checkpoint.  Per step k, with
+    u = gv_{k+1} + T gr_{k+1} and (h, g) = vjp_fp64(r_k, m, G, u):
+        gr_k = gr_{k+1} + T h,   gv_k = u,   dL/d(G m) += -T g.
+    Returns (dL/dr0, dL/dv0, dL/dm) for the incoming final-state gradients g_rK, g_vK."""
+    r = np.array(r0, dtype=np.float64).reshape(-1, 3)
+    v = np.array(v0, dtype=np.float64).reshape(-1, 3)
+    m = np.ascontiguousarray(m, dtype=np.float64)
+    starts = list(range(0, steps, every))
+    ckpt = []
+    for s0 in starts:
+        ckpt.append((r.copy(), v.copy()))
+        r, v = rollout_fp64(r, v, m, G, T, min(every, steps - s0), threads=threads)
+    gr = np.array(g_rK, dtype=np.float64).reshape(-1, 3)
+    gv = np.array(g_vK, dtype=np.float64).reshape(-1, 3)
+    g_gm = np.zeros(len(m))
+    for s0, (rc, vc) in zip(reversed(starts), reversed(ckpt)):
+        k = min(every, steps - s0)
+        states = [rc]
+        rr, vv = rc, vc
+        for _ in range(k - 1):
+            rr, vv = rollout_fp64(rr, vv, m, G, T, 1, threads=threads)
+            states.append(rr)
+        for rk in reversed(states):
+            u = gv + T * gr
+            h, g = vjp_fp64(rk, m, G, u, threads=threads)
+            gr = gr + T * h
+            gv = u
+            g_gm -= T * g
+    return gr, gv, G * g_gm
 
 
 # ---------------------------------------------------------------------------------

@@ -45,7 +45,9 @@ def test_single_step_against_oracle_vjp(gpu, pairs, store_a):
     r, v, m = compact(n, 3)
     rng = np.random.default_rng(1)
     c = rng.normal(size=(n, 3))
-    ro = Rollout([n], T, 1, every=1, adj_pairs=pairs, store_a=store_a)
+    # the forward in the plain FP32 arithmetic the backward pair kernels recompute with,
+    # so that the reversed state can be checked exactly
+    ro = Rollout([n], T, 1, every=1, adj_pairs=pairs, store_a=store_a, mode='fp32')
     assert ro.adj.pairs == pairs and ro.store_a == store_a
     dev = torch.device('cuda')
     rK, vK = ro.forward(torch.tensor(r, device=dev), torch.tensor(v, device=dev),
@@ -76,7 +78,7 @@ def test_single_step_batch_one_lane_per_row(gpu, store_a):
     v = np.concatenate([p[1] for p in parts])
     m = np.concatenate([p[2] for p in parts])
     c = np.random.default_rng(4).normal(size=r.shape)
-    ro = Rollout(sizes, T, 1, every=1, store_a=store_a)
+    ro = Rollout(sizes, T, 1, every=1, store_a=store_a, mode='fp32u')
     assert ro.adj.info.n_pad_total > 16384
     dev = torch.device('cuda')
     ro.forward(torch.tensor(r, device=dev), torch.tensor(v, device=dev),
@@ -169,3 +171,62 @@ def test_rollout_against_finite_differences(gpu):
         checks.append((which, g, fd))
     for which, g, fd in checks:
         assert abs(g - fd) <= 1e-4 * abs(fd) + 1e-12, (which, g, fd)
+
+
+def test_fp64_reference_gradients_match_oracle_adjoint(gpu):
+    """The checkpointed PyTorch FP64 autograd reference (used by the adjoint check at
+    the full configuration) against the oracle's FP64 discrete adjoint."""
+    from gravitation_gb300.adjoint import reference_gradients_fp64
+    n, steps = 256, 20
+    r, v, m = compact(n, 5)
+    t = r + 1.0
+    rk, _ = oracle.rollout_fp64(r, v, m, G_DEFAULT, T, steps)
+    g = (2.0 / n) * (rk - t)
+    want = oracle.adjoint_rollout_fp64(r, v, m, G_DEFAULT, T, steps, g, np.zeros_like(g),
+                                       every=6)
+    dev = torch.device('cuda')
+    tt = lambda x: torch.tensor(x, device=dev)  # noqa: E731
+    got = reference_gradients_fp64(tt(r), tt(v), tt(m), G_DEFAULT, T, steps, tt(g),
+                                   tt(np.zeros_like(g)), every=6)
+    for a, b in zip(got, want):
+        assert relerr(a.cpu().numpy(), b) < 1e-12
+
+
+# the differentiable-rollout configuration (uniform cube N = 4096, seed 3, checkpoint
+# every 32), shortened to 64 steps so that the CPU oracle's FP64 adjoint stays within
+# seconds; gradients of the mean squared distance to the target made by the same FP64
+# run with masses scaled by the seeded factor in [0.99, 1.01].  Errors are
+# ||g - g64|| / ||g64|| over every body.  Two tolerances:
+#   ADJ_TOL   the adjoint sweep itself, seeded with the exact FP64 dL/dr_K (its pair terms
+#             are FP32 on the FP64 state: measured 5e-9, 1e-10, 7e-6 on GB300);
+#   E2E_TOL   forward + adjoint, seeded from the rollout's own r_K: the loss is
+#             ill-conditioned (r_K - t is ~1e-9 of r_K), so the forward's force error
+#             dominates (near-corrected forward: measured 7e-5, 7e-5, 3e-5; plain FP32
+#             separations: 1e-3).
+ADJ_TOL = {'r0': 1e-7, 'v0': 1e-8, 'm': 5e-5}
+E2E_TOL = {'r0': 2e-4, 'v0': 2e-4, 'm': 1e-4}
+
+
+@pytest.mark.parametrize('store_a', [False, True])
+def test_config4_shortened_against_fp64_adjoint(gpu, store_a):
+    n, steps, every, seed = 4096, 64, 32, 3
+    r, v, m = uniform_cube(n, seed=seed)
+    f = mass_perturbation(n, seed)
+    t, _ = oracle.rollout_fp64(r, v, m * f, G_DEFAULT, T, steps)
+    rk64, _ = oracle.rollout_fp64(r, v, m, G_DEFAULT, T, steps)
+    g64 = (2.0 / n) * (rk64 - t)
+    want = oracle.adjoint_rollout_fp64(r, v, m, G_DEFAULT, T, steps, g64, np.zeros_like(g64),
+                                       every=every)
+    dev = torch.device('cuda')
+    ro = Rollout([n], T, steps, every, store_a=store_a)
+    assert ro.fwd.mode_name == 'fp32n'
+    rK, _ = ro.forward(torch.tensor(r, device=dev), torch.tensor(v, device=dev),
+                       torch.tensor(G_DEFAULT * m, device=dev))
+    seeds = {'exact': g64, 'own': (2.0 / n) * (rK.cpu().numpy() - t)}
+    for name, tol in (('exact', ADJ_TOL), ('own', E2E_TOL)):
+        g = torch.tensor(seeds[name], device=dev)
+        gr, gv, ggm = ro.backward(g, torch.zeros_like(g))
+        got = (gr.cpu().numpy(), gv.cpu().numpy(), G_DEFAULT * ggm.cpu().numpy())
+        errs = {k: relerr(a, b) for k, a, b in zip(('r0', 'v0', 'm'), got, want)}
+        for k, e in errs.items():
+            assert e < tol[k], (name, errs)
