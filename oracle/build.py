@@ -35,6 +35,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 # made from it travel)
 REF_ROOT = os.environ.get('GRAVITATION_REFERENCE') or '/root/reference'
 REF_KERNEL = os.path.join(REF_ROOT, 'src', 'gravitation', 'kernel')
+# the reference's Python package staged into the repository's git-ignored baseline/_ref
+# (sources included), so that it travels with the repository to the GPU host, where the
+# reference tree itself does not exist; its C and Cython kernels are compiled there
+BASELINE_REF = os.path.join(os.path.dirname(HERE), 'baseline', '_ref')
+STAGED_KERNEL = os.path.join(BASELINE_REF, 'gravitation', 'kernel')
 
 
 def _run(cmd):
@@ -94,38 +99,88 @@ def reference_present():
     return os.path.isfile(os.path.join(REF_KERNEL, '_base_.py'))
 
 
+def stage_reference(force=False):
+    """Where the reference tree is present: copy its Python package (src/gravitation,
+    sources included, no build products) to baseline/_ref/gravitation and render cy4's
+    Cython source to C beside it (cy4/core.c: the GPU host has no Cython).  pip cannot
+    install the reference offline on GCC 13: its c4a extension (_lib4_/lib.c, x86 SSE)
+    fails to compile (default(none) without PHY_G_SSE, lib.c:179-182), which stops the
+    whole build.  Returns the staged package directory, or None."""
+    if not reference_present():
+        return None
+    src = os.path.join(REF_ROOT, 'src', 'gravitation')
+    dst = os.path.join(BASELINE_REF, 'gravitation')
+    stamp = os.path.join(BASELINE_REF, '.staged')
+    if force or not os.path.isfile(stamp):
+        shutil.rmtree(dst, ignore_errors=True)
+        shutil.copytree(src, dst, ignore=shutil.ignore_patterns('*.so', '__pycache__', '*.pyc'))
+        with open(stamp, 'w') as f:
+            f.write(src + '\n')
+    # click, the reference front end's one pure-Python dependency that the GPU host lacks,
+    # from the local wheelhouse (the other absent imports have stand-ins, oracle/standins)
+    wheels = os.environ.get('GRAVITATION_WHEELHOUSE') or '/opt/wheelhouse'
+    if not os.path.isdir(os.path.join(BASELINE_REF, 'click')) and os.path.isdir(wheels):
+        try:
+            _run([sys.executable, '-m', 'pip', 'install', '--quiet', '--no-index', '--no-deps',
+                  '--find-links', wheels, '--target', BASELINE_REF, 'click'])
+        except (subprocess.CalledProcessError, OSError):
+            pass
+    pyx = os.path.join(dst, 'kernel', 'cy4', 'core.pyx')
+    c_file = os.path.join(dst, 'kernel', 'cy4', 'core.c')
+    if os.path.isfile(pyx) and (force or not _newer(c_file, pyx)):
+        try:
+            _run([sys.executable, '-m', 'cython', '-3', pyx, '-o', c_file])
+        except (subprocess.CalledProcessError, OSError):
+            pass
+    return dst
+
+
+def staged_reference():
+    """True when baseline/_ref holds the staged reference package."""
+    return os.path.isfile(os.path.join(STAGED_KERNEL, '_base_.py'))
+
+
 def build_reference(force=False):
-    """Compile the reference's c1a C kernel and cy4 Cython kernel into oracle/_ref/.
+    """Compile the reference's c1a C kernel and cy4 Cython kernel, on this host, from the
+    staged reference package (stage_reference; here, or on the GPU host after the push):
+    in place, where the reference's own wrappers load them (_lib1_/lib.so, cy4/core*.so),
+    and as copies in oracle/_ref/ (lib1.so, cy4/core*.so).  The reference's compiler
+    flags are used (setup.py:87-118) minus the x86-only ones on other hosts.
 
     Returns a dict name -> path (or an error string) for what was attempted.
     """
     result = {}
-    if not reference_present():
+    stage_reference()
+    if not staged_reference():
         return result
     refdir = os.path.join(HERE, '_ref')
     os.makedirs(refdir, exist_ok=True)
-    lib1_src = os.path.join(REF_KERNEL, '_lib1_', 'lib.c')
+    lib1_src = os.path.join(STAGED_KERNEL, '_lib1_', 'lib.c')
+    lib1_inplace = os.path.join(STAGED_KERNEL, '_lib1_', 'lib.so')
     lib1_out = os.path.join(refdir, 'lib1.so')
     try:
-        if force or not _newer(lib1_out, lib1_src):
+        if force or not _newer(lib1_inplace, lib1_src):
             flags = ['-std=gnu11', '-fPIC', '-Wall'] + reference_flags()
-            _run(['gcc'] + flags + ['-shared', lib1_src, '-o', lib1_out, '-lm'])
+            _run(['gcc'] + flags + ['-shared', lib1_src, '-o', lib1_inplace, '-lm'])
+        shutil.copyfile(lib1_inplace, lib1_out)
         result['lib1'] = lib1_out
     except (subprocess.CalledProcessError, OSError) as e:
         result['lib1'] = 'unbuildable: %s' % e
-    cy4_src = os.path.join(REF_KERNEL, 'cy4', 'core.pyx')
-    cy4_dir = os.path.join(refdir, 'cy4')
+    cy4_dir_src = os.path.join(STAGED_KERNEL, 'cy4')
+    cy4_c = os.path.join(cy4_dir_src, 'core.c')
     suffix = sysconfig.get_config_var('EXT_SUFFIX')
+    cy4_inplace = os.path.join(cy4_dir_src, 'core' + suffix)
+    cy4_dir = os.path.join(refdir, 'cy4')
     cy4_out = os.path.join(cy4_dir, 'core' + suffix)
     try:
-        if force or not _newer(cy4_out, cy4_src):
-            os.makedirs(cy4_dir, exist_ok=True)
-            with tempfile.TemporaryDirectory() as tmp:
-                c_file = os.path.join(tmp, 'core.c')
-                _run([sys.executable, '-m', 'cython', '-3', cy4_src, '-o', c_file])
-                inc = sysconfig.get_paths()['include']
-                _run(['gcc', '-O3', '-fPIC', '-shared', '-fopenmp', '-I', inc,
-                      c_file, '-o', cy4_out, '-lm'])
+        if not os.path.isfile(cy4_c):
+            raise OSError('cy4/core.c not rendered (no Cython where the package was staged)')
+        if force or not _newer(cy4_inplace, cy4_c):
+            inc = sysconfig.get_paths()['include']
+            _run(['gcc', '-O3', '-fPIC', '-shared', '-fopenmp', '-I', inc,
+                  cy4_c, '-o', cy4_inplace, '-lm'])
+        os.makedirs(cy4_dir, exist_ok=True)
+        shutil.copyfile(cy4_inplace, cy4_out)
         result['cy4'] = cy4_out
     except (subprocess.CalledProcessError, OSError) as e:
         result['cy4'] = 'unbuildable: %s' % e

@@ -68,40 +68,7 @@ def test_reference_inventory_discovers_gb1(tmp_path):
     assert 'OK' in res.stdout
 
 
-_FAKE_H5PY = '''
-"""In-memory stand-in for the h5py calls of gravitation/lib/simulation.py (File,
-create_group, create_dataset, attrs, item access), persisted with pickle so that a file
-written by one call can be read by the next.  Test double only: h5py is absent here."""
-import os, pickle
-import numpy as np
-
-class _Group(dict):
-    def __init__(self):
-        super().__init__()
-        self.attrs = {}
-    def create_group(self, name):
-        if name in self:
-            raise ValueError('group %s exists' % name)
-        self[name] = _Group()
-        return self[name]
-    def create_dataset(self, name, shape, dtype):
-        self[name] = np.zeros(shape, dtype=np.dtype(dtype))
-        return self[name]
-
-class File(_Group):
-    def __init__(self, fn, mode='r'):
-        super().__init__()
-        self._fn, self._mode = fn, mode
-        if os.path.exists(fn):
-            with open(fn, 'rb') as f:
-                self.update(pickle.load(f))
-        elif mode == 'r':
-            raise OSError(fn)
-    def close(self):
-        if self._mode != 'r':
-            with open(self._fn, 'wb') as f:
-                pickle.dump(dict(self), f)
-'''
+_FAKE_H5PY = open(os.path.join(ROOT, 'oracle', 'standins', 'h5py.py')).read()
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_SRC), reason='reference tree not present')
@@ -256,3 +223,16 @@ def test_default_stage2_matches_oracle():
     r2, v2 = oracle.stage2_fp64(r, v, a, 123.0)
     assert np.array_equal(np.array([pm._r for pm in u]), r2)
     assert np.array_equal(np.array([pm._v for pm in u]), v2)
+
+
+def test_reference_cli_loads_with_gb1_among_its_kernels(tmp_path):
+    """The reference's command-line front end (staged in baseline/_ref) imports with the
+    stand-ins of oracle/standins and offers gb1 as a kernel of its worker command."""
+    from oracle import frontend
+    ok, why = frontend.available()
+    if not ok:
+        pytest.skip(why)
+    env = frontend.prepare(str(tmp_path))
+    res = frontend.cli(env, ['worker', '--help'], 300, str(tmp_path))
+    assert res.returncode == 0, res.stderr[-2000:]
+    assert 'gb1' in res.stdout
