@@ -519,6 +519,19 @@ def run_ours(args):
     if not args.no_adjoint:
         from gravitation_gb300.workloads import run_adjoint
         adjoint = run_adjoint(tuner=default_tuner(), device=local)
+        # forward + adjoint against forward beyond the specified size (fewer steps, same
+        # checkpoint interval)
+        adjoint['by_n'] = {}
+        for n_adj, steps_adj in ((8192, 256), (16384, 128)):
+            res = run_adjoint(n=n_adj, steps=steps_adj, tuner=default_tuner(), device=local)
+            adjoint['by_n'][str(n_adj)] = {
+                'steps': steps_adj,
+                'ratio_fwd_plus_adjoint_over_fwd': res['ratio_fwd_plus_adjoint_over_fwd'],
+                'ratio_kept_accelerations': res['kept_accelerations'][
+                    'ratio_fwd_plus_adjoint_over_fwd'],
+                'fwd_adjoint_steps_per_s': res['fwd_adjoint_steps_per_s'],
+                'forward_ms': res['forward_ms'], 'forward_adjoint_ms': res['forward_adjoint_ms'],
+                'forward_mode': res['forward_mode']}
 
     precision = None
     if rank == 0 and not args.no_precision:

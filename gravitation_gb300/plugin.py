@@ -19,6 +19,8 @@ Kernel options (keyword arguments of the constructor, kept in self._meta):
   precision  'fp32n' | 'fp32un' | 'fp32' | 'fp32u' | 'fp32c' | 'fp32cu' | 'fp64'   default
              from dtype: 'float32' -> fp32n below 8192 bodies, fp32un from there on while
              its partial-sum slots fit an eighth of the GPU's memory (~1.7 M bodies);
+             fp32c / fp32cu instead when more than 1e-3 of sampled pairs are near
+             (default_mode, near_pair_fraction: discs, dense clusters far out);
              'float64' -> fp64.  fp32/fp32u: plain FP32 separations (fp32u visits each
              pair once); fp32n/fp32un: the same plus double-single separations for near
              pairs (closer than |x|/20), which keeps every body within ~1e-6 of the FP64
@@ -44,6 +46,7 @@ Kernel options (keyword arguments of the constructor, kept in self._meta):
              the point masses are made on first access (see _MirrorMasses)
 """
 
+import ctypes
 import sys
 
 import numpy as np
@@ -60,16 +63,52 @@ _DTYPE_MODE = {'float32': 'fp32n', 'float64': 'fp64'}
 UNIQUE_PAIRS_FROM_N = 8192
 
 
-def default_mode(dtype, n, budget=None):
+# Above this fraction of near pairs the near-corrected kernels spend more time on their
+# correction path than double-single separations for every pair cost (fp32c / fp32cu,
+# ~1.4x the plain loop): the near path then runs on most steps of the loop.
+NEAR_DS_FRACTION = 1e-3
+
+
+def near_pair_fraction(r, samples=1 << 16, seed=0, rows=8):
+    """Fraction of `samples` seeded random pairs (i != j) of positions r (n x >=3) that
+    the near-corrected kernels treat as near: |r_j - r_i| below m / GRAV_NEAR_KAPPA,
+    where m is the largest |coordinate| among the `rows` bodies a thread holds (i and
+    rows - 1 others drawn at random, as the kernels' rows are spread over the body
+    order).  About 5e-5 for the uniform cube of the benchmark; dense clusters far from
+    the origin, and discs whose outer bodies set the radius for the inner ones, reach
+    1e-3 and more."""
+    r = np.asarray(r, dtype=np.float64)[:, :3]
+    n = len(r)
+    if n < 2:
+        return 0.0
+    rng = np.random.default_rng(seed)
+    i = rng.integers(n, size=samples)
+    j = rng.integers(n - 1, size=samples)
+    j += j >= i
+    d2 = ((r[j] - r[i]) ** 2).sum(1)
+    scale = np.abs(r).max(1)
+    others = rng.integers(n, size=(samples, max(rows - 1, 0)))
+    m = np.maximum(scale[i], scale[others].max(1) if rows > 1 else 0.0)
+    thr = (m / _lib.GRAV_NEAR_KAPPA) ** 2
+    return float((d2 < thr).mean())
+
+
+def default_mode(dtype, n, budget=None, r=None):
     """Precision mode for a dtype and body count: float32 runs on unique pairs from
     UNIQUE_PAIRS_FROM_N bodies while the unique-pair plan's partial-sum slots fit the
     slot budget (engine.slot_budget_bytes, or `budget` bytes), on all pairs otherwise
-    (above ~1.7 million bodies on a GB300)."""
+    (above ~1.7 million bodies on a GB300); near pairs are corrected (fp32n / fp32un),
+    or, given positions r whose near-pair fraction exceeds NEAR_DS_FRACTION, every pair
+    takes double-single separations (fp32c / fp32cu).  Both keep the forces within
+    1e-5 of FP64."""
     mode = _DTYPE_MODE.get(str(dtype))
     if mode == 'fp32n' and n >= UNIQUE_PAIRS_FROM_N:
         from .engine import pair_plan_fits
         if pair_plan_fits([n], budget, mode='fp32un'):
             mode = 'fp32un'
+    if mode in ('fp32n', 'fp32un') and r is not None and \
+            near_pair_fraction(r) > NEAR_DS_FRACTION:
+        mode = {'fp32n': 'fp32c', 'fp32un': 'fp32cu'}[mode]
     return mode
 
 
@@ -143,7 +182,10 @@ class GB300Stages:
             from .tune import default_tuner
             tuner = default_tuner()
         device = meta.get('device')
-        self._gb = Engine([n], float(self._T), mode=mode, tile=tile, device=device, tuner=tuner)
+
+        def make_engine(m):
+            return Engine([n], float(self._T), mode=m, tile=tile, device=device, tuner=tuner)
+        self._gb = make_engine(mode)
         dev = self._gb.device
         # pinned FP64 host mirror (x, y, z, G*m) / (vx, vy, vz, 0) / (ax, ay, az, 0)
         pin = torch.cuda.is_available()
@@ -179,6 +221,18 @@ class GB300Stages:
                 pm._r = hr[i, :3]
                 pm._v = hv[i, :3]
                 pm._a = ha[i, :3]
+        if not meta.get('precision') and mode in ('fp32n', 'fp32un'):
+            # with the positions known: dense configurations far from the origin take
+            # double-single separations for every pair (default_mode)
+            chosen = default_mode(self._dtype, n, r=hr)
+            if chosen != mode:
+                if tile is not None and not self._gb.lib.grav_tile_supported(
+                        _lib.MODES[chosen], ctypes.byref(tile)):
+                    chosen = mode
+            if chosen != mode:
+                self._gb = make_engine(chosen)
+                self._gb.set_state(hr[:, :3], hv[:, :3], hr[:, 3], stream=self._gb_stream)
+                self._gb_stream.synchronize()
         self._gb_a_dirty = False
         # host_sync='full' keeps the state in the host mirror itself when the device can
         # address it: prepare and stage 2 read and write it in place

@@ -60,7 +60,7 @@ def run_adjoint(n=4096, steps=1000, every=32, seed=3, reps=3, tuner=None, device
         ro.adj.raise_on_device_error()
         ro.fwd.raise_on_device_error()
         f, t = min(fwd_ms[1:]), min(tot_ms[1:])
-        return {'forward_ms': f, 'forward_adjoint_ms': t,
+        return {'forward_ms': f, 'forward_adjoint_ms': t, 'forward_mode': ro.fwd.mode_name,
                 'ratio_fwd_plus_adjoint_over_fwd': t / f,
                 'fwd_adjoint_steps_per_s': steps / (t * 1e-3),
                 'forward_tile': [ro.fwd.tile.bpt, ro.fwd.tile.threads, ro.fwd.tile.jtile,
@@ -78,7 +78,7 @@ def run_adjoint(n=4096, steps=1000, every=32, seed=3, reps=3, tuner=None, device
     out['kept_accelerations'] = measure(True, store_a=True)
     out.update({k: out['graphs'][k] for k in ('forward_ms', 'forward_adjoint_ms',
                                              'ratio_fwd_plus_adjoint_over_fwd',
-                                             'fwd_adjoint_steps_per_s')})
+                                             'fwd_adjoint_steps_per_s', 'forward_mode')})
     return out
 
 

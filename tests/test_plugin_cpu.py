@@ -236,3 +236,21 @@ def test_reference_cli_loads_with_gb1_among_its_kernels(tmp_path):
     res = frontend.cli(env, ['worker', '--help'], 300, str(tmp_path))
     assert res.returncode == 0, res.stderr[-2000:]
     assert 'gb1' in res.stdout
+
+
+def test_near_pair_fraction_picks_the_precision_mode():
+    """float32 with positions known: the near-corrected modes for configurations with few
+    near pairs (the uniform cube), double-single separations for every pair where near
+    pairs are common (two dense clusters far from the origin)."""
+    from gravitation_gb300 import build as gbuild
+    gbuild.build()
+    from gravitation_gb300.plugin import default_mode, near_pair_fraction, NEAR_DS_FRACTION
+    from gravitation_gb300.scenarios import plummer_pair, uniform_cube
+    cube = uniform_cube(16384, seed=0)[0]
+    pair = plummer_pair(16384, seed=2)[0]
+    assert near_pair_fraction(cube) < NEAR_DS_FRACTION < near_pair_fraction(pair)
+    assert default_mode('float32', 16384, r=cube) == 'fp32un'
+    assert default_mode('float32', 16384, r=pair) == 'fp32cu'
+    assert default_mode('float32', 4096, r=pair[:4096]) == 'fp32c'
+    assert default_mode('float64', 16384, r=pair) == 'fp64'
+    assert near_pair_fraction(cube[:1]) == 0.0
