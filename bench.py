@@ -688,8 +688,12 @@ def run_workload(args):
             torch.cuda.synchronize()
             eng.raise_on_device_error()
             return 0
+        tile = None
+        if args.tile:
+            from gravitation_gb300 import _lib
+            tile = _lib.Tile(*(int(x) for x in args.tile.split(',')), 0)
         res = workloads.run_batched(steps=100, warmup=args.warmup, mode=args.mode,
-                                    tuner=default_tuner())
+                                    tuner=default_tuner(), tile=tile)
     else:
         raise SystemExit('unknown workload %r' % args.workload)
     res['workload_name'] = args.workload

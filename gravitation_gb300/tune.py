@@ -8,7 +8,8 @@ a tuned tile whatever their exact sizes) -- every compiled
 tile shape, at 1, 1/2 and 1/4 of
 the resident persistent grid, is timed as full steps replayed from a CUDA graph (CUDA
 events, at least ~2 ms of steps) on a seeded synthetic state of that size, and the
-fastest is cached as JSON.
+fastest is cached as JSON (the four fastest of that pass timed again, longer, and the
+best of those kept).
 
 Cache robustness: an unreadable or malformed cache file is ignored (and rewritten),
 entries from another library build (different source hash) or naming a tile that is
@@ -140,7 +141,7 @@ class Tuner:
         per row for stage 2, which at a few thousand bodies is worth as much.  Above
         2^38 interactions per step a replay holds one step instead of `reps`."""
         import torch
-        from .engine import Engine, occupancy, tile_list
+        from .engine import Engine, make_plan, occupancy, tile_list
         from .scenarios import uniform_cube
         sizes = [int(s) for s in sizes]
         rs, vs, ms = [], [], []
@@ -158,6 +159,32 @@ class Tuner:
             # steps of 0.1 s and more (above ~500k bodies): one step per replay is
             # already far above the timing noise, and keeps tuning to about a minute
             reps = 1
+        def time_tile(t, min_ms):
+            """ms per step of tile t: full steps replayed from a CUDA graph, enough
+            replays for about `min_ms` of steps (short steps time noisily)."""
+            eng = Engine(sizes, 1.0, mode=mode, tile=t, device=dev_info.index)
+            eng.set_state(r, v, gm)
+            s = torch.cuda.current_stream(eng.device)
+            g = eng.capture_graph(reps)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            g.replay()
+            e0.record(s)
+            g.replay()
+            e1.record(s)
+            e1.synchronize()
+            k = max(1, min(100, int(min_ms / max(e0.elapsed_time(e1), 1e-3))))
+            e0.record(s)
+            for _ in range(k):
+                g.replay()
+            e1.record(s)
+            e1.synchronize()
+            eng.raise_on_device_error()
+            out = e0.elapsed_time(e1) / (k * reps)
+            del g, eng
+            return out
+
+        timed = []
         for cand in tile_list(mode):
             occ = occupancy(mode, cand, dev_info.index)
             if occ <= 0:
@@ -165,33 +192,21 @@ class Tuner:
             for gf in grid_factors:
                 grid = max(1, int(dev_info.sm_count * occ * gf))
                 t = _lib.Tile(cand.bpt, cand.threads, cand.jtile, grid)
-                eng = Engine(sizes, 1.0, mode=mode, tile=t, device=dev_info.index)
-                key = (t.bpt, t.threads, t.jtile, eng.info.grid)  # the plan caps the grid
+                pinfo = make_plan(sizes, 1.0, t, mode)[0]
+                key = (t.bpt, t.threads, t.jtile, pinfo.grid)  # the plan caps the grid
                 if key in seen:
                     continue
                 seen.add(key)
-                eng.set_state(r, v, gm)
-                s = torch.cuda.current_stream(eng.device)
-                g = eng.capture_graph(reps)
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                g.replay()
-                e0.record(s)
-                g.replay()
-                e1.record(s)
-                e1.synchronize()
-                # replay enough times for ~2 ms of steps: short steps time noisily
-                k = max(1, min(100, int(2.0 / max(e0.elapsed_time(e1), 1e-3))))
-                e0.record(s)
-                for _ in range(k):
-                    g.replay()
-                e1.record(s)
-                e1.synchronize()
-                eng.raise_on_device_error()
-                ms_ = e0.elapsed_time(e1) / (k * reps)
-                if best is None or ms_ < best[0]:
-                    best = (ms_, _lib.Tile(t.bpt, t.threads, t.jtile, eng.info.grid))
-                del g, eng
+                # the grid as tried, not as this size's plan capped it: the entry serves
+                # every size of the bucket, each plan capping the grid at its own units
+                timed.append((time_tile(t, 2.0), t))
+        # a second pass over the closest candidates, with longer timings and in another
+        # order: a single short timing picked tiles 10 % off the best on GB300
+        timed.sort(key=lambda x: x[0])
+        for ms_, t in timed[:4][::-1]:
+            again = min(time_tile(t, 6.0), time_tile(t, 6.0))
+            if best is None or again < best[0]:
+                best = (again, t)
         if best is None:
             raise RuntimeError('no tile shape could be timed for mode %s' % mode)
         self.store(mode, sizes, dev_info, best[1], best[0])

@@ -357,7 +357,7 @@ def _loop_timings(engines, stream, dev, warmup, loop_steps):
 
 
 def run_batched(steps=100, warmup=3, mode='fp32un', n_univ=256, seed=1, loop_steps=10,
-                tuner=None, device=None):
+                tuner=None, device=None, tile=None):
     """Batched step vs the per-universe loop.  Returns a dict of measurements.
 
     The batch runs in `mode` with the tile the autotuner picks for the batch.  The loop
@@ -376,7 +376,7 @@ def run_batched(steps=100, warmup=3, mode='fp32un', n_univ=256, seed=1, loop_ste
     dev = torch.device('cuda', torch.cuda.current_device() if device is None else device)
     stream = torch.cuda.current_stream(dev)
 
-    eng = Engine(sizes, T_DEFAULT, mode=mode, tuner=tuner, device=dev.index)
+    eng = Engine(sizes, T_DEFAULT, mode=mode, tile=tile, tuner=tuner, device=dev.index)
     eng.set_state(r, v, gm)
     graph = eng.capture_graph(1)
     for _ in range(warmup):
