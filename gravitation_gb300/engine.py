@@ -211,7 +211,7 @@ class Engine:
         self.T = list(T) if np.ndim(T) else [float(T)] * len(self.sizes)
         if tile is None:
             if tuner is not None:
-                tile = tuner.choose(self.mode_name, self.sizes, self.dev_info)
+                tile = tuner.choose(self.mode_name, self.sizes, self.dev_info, T=self.T)
             else:
                 tile = default_tile(self.mode_name, self.sizes, self.dev_info.index)
         elif tile.grid <= 0:

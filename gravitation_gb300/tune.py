@@ -119,8 +119,9 @@ class Tuner:
             self.save()
 
     # ---- tuning ---------------------------------------------------------------------
-    def choose(self, mode, sizes, dev_info, tune_if_missing=None):
-        """Tile for the workload: cached, else tuned (if enabled), else the default."""
+    def choose(self, mode, sizes, dev_info, tune_if_missing=None, T=None):
+        """Tile for the workload: cached, else tuned (if enabled, with time step T), else
+        the default."""
         from .engine import default_tile
         t = self.lookup(mode, sizes, dev_info)
         if t is not None:
@@ -130,16 +131,21 @@ class Tuner:
         if tune_if_missing is None:
             tune_if_missing = os.environ.get('GRAV_AUTOTUNE', '1') != '0'
         if tune_if_missing:
-            return self.tune(mode, sizes, dev_info)
+            return self.tune(mode, sizes, dev_info, T=T)
         return default_tile(mode, sizes, dev_info.index)
 
-    def tune(self, mode, sizes, dev_info, reps=5, grid_factors=(1, 0.5, 0.25)):
+    def tune(self, mode, sizes, dev_info, reps=5, grid_factors=(1, 0.5, 0.25), T=None):
         """Time every compiled tile shape, with the persistent grid at each of
         `grid_factors` x (SMs x resident CTAs), on a seeded state and cache the fastest.
         What is timed is the full step (stage 1 + stage 2) replayed from a CUDA graph: a
         smaller grid gives each CTA more work units but leaves fewer partial-sum slots
         per row for stage 2, which at a few thousand bodies is worth as much.  Above
-        2^38 interactions per step a replay holds one step instead of `reps`."""
+        2^38 interactions per step a replay holds one step instead of `reps`.  The steps
+        use the workload's time step T (one per universe or one for all; default the
+        reference's 1e3): the near-pair kernels' cost follows the state, and a uniform
+        cube streaming for a few steps at T = 1e3 takes the shape of its velocity
+        distribution, where more pairs are near than in the cube (at T = 1 nothing
+        moves, and the tiles with 8 rows per thread timed 12 % faster than they run)."""
         import torch
         from .engine import Engine, make_plan, occupancy, tile_list
         from .scenarios import uniform_cube
@@ -155,6 +161,7 @@ class Tuner:
         gm = np.concatenate(ms) if ms else np.zeros(0)
         best = None
         seen = set()
+        step_T = 1e3 if T is None else T
         if sum(n * n for n in sizes) >= 1 << 38:
             # steps of 0.1 s and more (above ~500k bodies): one step per replay is
             # already far above the timing noise, and keeps tuning to about a minute
@@ -162,7 +169,7 @@ class Tuner:
         def time_tile(t, min_ms):
             """ms per step of tile t: full steps replayed from a CUDA graph, enough
             replays for about `min_ms` of steps (short steps time noisily)."""
-            eng = Engine(sizes, 1.0, mode=mode, tile=t, device=dev_info.index)
+            eng = Engine(sizes, step_T, mode=mode, tile=t, device=dev_info.index)
             eng.set_state(r, v, gm)
             s = torch.cuda.current_stream(eng.device)
             g = eng.capture_graph(reps)
