@@ -200,14 +200,9 @@ __device__ __forceinline__ void rows_tile(const float4* __restrict__ sj,
 	const float4* __restrict__ rowlo, int tid, int T)
 {
 	static_assert(JT % 32 == 0, "j-tiles of whole 32-body groups");
-	// with one or two rows per thread a bit per step costs as much as the pair test
-	// itself: there the steps' tests are or-ed and a chunk with a near pair re-checks all
-	// its 32 steps on the cold path (a chunk holds 32 x 32 B pairs, so that is rare)
-	constexpr bool WHOLE_CHUNK = B <= 2;
 #pragma unroll 1
 	for (int j0 = 0; j0 < JT; j0 += 32) {
 		uint32_t nmask = 0;
-		bool nany = false;
 #pragma unroll 4
 		for (int jj = 0; jj < 32; ++jj) {
 			const float4 pj = sj[j0 + jj];
@@ -234,12 +229,10 @@ __device__ __forceinline__ void rows_tile(const float4* __restrict__ sj,
 				fz[k] = fmaf(dz, w, fz[k]);
 			}
 			if (NEAR && !SELF) near = rmin < thr;
-			if (NEAR && WHOLE_CHUNK) nany |= near;
-			if (NEAR && !WHOLE_CHUNK && near) nmask |= 1u << jj;
+			if (NEAR && near) nmask |= 1u << jj;
 		}
 		if (NEAR) {
-			uint32_t todo = WHOLE_CHUNK ? (__any_sync(0xffffffffu, nany) ? 0xffffffffu : 0u)
-			                            : __reduce_or_sync(0xffffffffu, nmask);
+			uint32_t todo = __reduce_or_sync(0xffffffffu, nmask);
 			while (todo) {
 				const int jj = __ffs(todo) - 1;
 				todo &= todo - 1;
