@@ -279,12 +279,14 @@ def run_precision(n=16384, steps=10000, every=100, seed=2,
     return out
 
 
-def run_sweep(sizes=None, mode=None, reps=5, tuner=None, device=None):
+def run_sweep(sizes=None, mode=None, reps=50, tuner=None, device=None):
     """Interactions/s of the single-universe step over an N sweep (2^4 .. 2^17), with
     the state in HBM.  mode None: the plugin's float32 default at each size (all pairs
     below 8192 bodies, unique pairs from there, near pairs corrected).  Below 8192 bodies
     one graph replay holds 20 steps, so that the host's graph-launch rate does not set
-    the measured step time; above, one step per replay."""
+    the measured step time; above, one step per replay.  At least `reps` steps are
+    timed: the near-pair kernels' cost follows the state, which at the reference's time
+    step streams from the cube towards the shape of its velocity distribution."""
     from .plugin import default_mode
     from .scenarios import uniform_cube
     sizes = sizes or [2 ** k for k in range(4, 18)]
