@@ -527,7 +527,8 @@ def run_ours(args):
             adjoint['by_n'][str(n_adj)] = {
                 'steps': steps_adj,
                 'ratio_fwd_plus_adjoint_over_fwd': res['ratio_fwd_plus_adjoint_over_fwd'],
-                'ratio_kept_accelerations': res['kept_accelerations'][
+                'backward_kernel': res['graphs']['backward_kernel'],
+                'ratio_recomputed_accelerations': res['recomputed_accelerations'][
                     'ratio_fwd_plus_adjoint_over_fwd'],
                 'fwd_adjoint_steps_per_s': res['fwd_adjoint_steps_per_s'],
                 'forward_ms': res['forward_ms'], 'forward_adjoint_ms': res['forward_adjoint_ms'],

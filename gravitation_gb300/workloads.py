@@ -25,9 +25,10 @@ from .scenarios import G_DEFAULT, T_DEFAULT, batch_universes
 def run_adjoint(n=4096, steps=1000, every=32, seed=3, reps=3, tuner=None, device=None):
     """Forward rollout vs forward + adjoint (gradients of the mean squared distance to a
     target made by the same run with masses scaled by a seeded factor in [0.99, 1.01]).
-    Returns timings and the steps/s of forward+adjoint: checkpoints every `every` steps
-    with stage 1 recomputed in the backward sweep (graph-replayed and launched), and,
-    beside it, the variant that keeps the forward's accelerations (store_a)."""
+    Returns timings and the steps/s of forward+adjoint with the Rollout's defaults
+    (checkpoints every `every` steps, the forward's accelerations kept where they fit:
+    graph-replayed and launched) and, beside it, the variant that recomputes stage 1
+    in the backward sweep instead (store_a=False)."""
     from .adjoint import Rollout
     from .scenarios import mass_perturbation, uniform_cube
     r, v, m = uniform_cube(n, seed=seed)
@@ -38,7 +39,7 @@ def run_adjoint(n=4096, steps=1000, every=32, seed=3, reps=3, tuner=None, device
     v0 = torch.tensor(v, device=dev)
     stream = torch.cuda.current_stream(dev)
 
-    def measure(graphs, store_a=False):
+    def measure(graphs, store_a='auto'):
         ro = Rollout([n], T_DEFAULT, steps, every, device=dev.index, tuner=tuner,
                      graphs=graphs, store_a=store_a)
         rt, _ = ro.forward(r0, v0, gm_t)
@@ -75,7 +76,7 @@ def run_adjoint(n=4096, steps=1000, every=32, seed=3, reps=3, tuner=None, device
            'launches_per_step': {'forward': 2, 'adjoint': 2}}
     out['graphs'] = measure(True)
     out['launched'] = measure(False)
-    out['kept_accelerations'] = measure(True, store_a=True)
+    out['recomputed_accelerations'] = measure(True, store_a=False)
     out.update({k: out['graphs'][k] for k in ('forward_ms', 'forward_adjoint_ms',
                                              'ratio_fwd_plus_adjoint_over_fwd',
                                              'fwd_adjoint_steps_per_s', 'forward_mode')})
