@@ -13,7 +13,7 @@ own scenarios are generated too.
              the GPU tests pin the FP64 mode to the CPU FP64 oracle at 1e-12
   precision  the Plummer-pair stress (N = 16384, 1000 steps): force errors over every
              body at the first and last step and energy / momentum drift, per mode
-  sweep      the step over N = 2^10 .. 2^17 in the plugin's float32 default at each size,
+  sweep      the step over N = 2^4 .. 2^17 in the plugin's float32 default at each size,
              with the CPU baseline beside every size
 
   value      pair interactions per second (N^2 per step), device-timed steps with the
@@ -396,10 +396,11 @@ def compact_precision(device):
 
 
 def compact_sweep(tuner, cpu=True):
-    """Single-universe step over N = 2^10 .. 2^17 in the plugin's float32 default at each
-    size, device-timed, with the CPU baseline (the port on the host cores) beside it."""
+    """Single-universe step over N = 2^4 .. 2^17 in the plugin's float32 default at each
+    size (up to 512 bodies the single-launch step), device-timed, with the CPU baseline
+    (the port on the host cores) beside it."""
     from gravitation_gb300.workloads import run_sweep
-    rows = run_sweep(sizes=[2 ** k for k in range(10, 18)], tuner=tuner)
+    rows = run_sweep(sizes=[2 ** k for k in range(4, 18)], tuner=tuner)
     for row in rows:
         if cpu:
             cv, threads, _ = cpu_baseline_run(row['n'], 0, 0.3, runs=2)

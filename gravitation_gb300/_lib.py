@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, 'libgravgb300.so')
 
 # ---- constants (mirror of the header) -------------------------------------------
-GRAV_ABI_VERSION = 4
+GRAV_ABI_VERSION = 5
 GRAV_OK = 0
 GRAV_E_ARG = -1
 GRAV_E_TILE = -2
@@ -33,6 +33,7 @@ GRAV_MODE_FP32CU = 4
 GRAV_MODE_FP32N = 5
 GRAV_MODE_FP32UN = 6
 GRAV_NEAR_KAPPA = 20
+GRAV_FUSED_MAX_N = 4096
 MODES = {'fp32': GRAV_MODE_FP32, 'fp32c': GRAV_MODE_FP32C, 'fp64': GRAV_MODE_FP64,
          'fp32u': GRAV_MODE_FP32U, 'fp32cu': GRAV_MODE_FP32CU, 'fp32n': GRAV_MODE_FP32N,
          'fp32un': GRAV_MODE_FP32UN}
@@ -127,6 +128,12 @@ _DECLS = {
     'grav_stage1': (ctypes.c_int, [_P(Batch), ctypes.c_void_p]),
     'grav_stage2': (ctypes.c_int, [_P(Batch), ctypes.c_int, ctypes.c_void_p]),
     'grav_step': (ctypes.c_int, [_P(Batch), ctypes.c_int, ctypes.c_void_p]),
+    'grav_fused_supported': (ctypes.c_int, [ctypes.c_int, ctypes.c_int32, ctypes.c_int32,
+                                            ctypes.c_int32]),
+    'grav_fused_occupancy': (ctypes.c_int, [ctypes.c_int, ctypes.c_int32, ctypes.c_int32,
+                                            ctypes.c_int32, _P(ctypes.c_int32)]),
+    'grav_step_fused': (ctypes.c_int, [_P(Batch), ctypes.c_int, ctypes.c_int32, ctypes.c_int32,
+                                       ctypes.c_void_p, ctypes.c_void_p]),
     'grav_fp32_peak_probe': (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                                             ctypes.c_void_p]),
     'grav_energy': (ctypes.c_int, [_P(Batch), ctypes.c_void_p, ctypes.c_void_p]),

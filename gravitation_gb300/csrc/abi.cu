@@ -417,6 +417,50 @@ int grav_step(const grav_batch* b, int flags, void* stream)
 	return grav_stage2(b, flags & ~GRAV_S2_PREPARE, stream);
 }
 
+int grav_fused_supported(int mode, int32_t n, int32_t threads, int32_t rows)
+{
+	if (mode != GRAV_MODE_FP32 && mode != GRAV_MODE_FP32C && mode != GRAV_MODE_FP32N) return 0;
+	if (n < 0 || n > GRAV_FUSED_MAX_N || rows < 1 || rows > threads) return 0;
+	return grav::find_fused(mode, threads) != nullptr ? 1 : 0;
+}
+
+int grav_fused_occupancy(int mode, int32_t n, int32_t threads, int32_t rows,
+	int32_t* ctas_per_sm)
+{
+	if (!ctas_per_sm) return fail(GRAV_E_ARG, "ctas_per_sm is NULL");
+	if (!grav_fused_supported(mode, n, threads, rows))
+		return fail(GRAV_E_TILE, "no single-launch step for mode %d, n %d, %d threads, %d rows",
+			mode, n, threads, rows);
+	int blocks = 0;
+	if (grav::fused_occupancy(mode, n, threads, rows, &blocks) != 0)
+		return fail(GRAV_E_CUDA, "occupancy query of the single-launch step failed");
+	*ctas_per_sm = blocks;
+	return ok();
+}
+
+int grav_step_fused(const grav_batch* b, int flags, int32_t threads, int32_t rows,
+	int32_t* sync, void* stream)
+{
+	int rc = check_batch(b);
+	if (rc) return rc;
+	if (b->n_univ != 1) return fail(GRAV_E_ARG, "the single-launch step takes one universe (n_univ = %d)", b->n_univ);
+	if (!sync) return fail(GRAV_E_ARG, "sync is NULL");
+	if (flags & ~(GRAV_S2_INTEGRATE | GRAV_S2_WRITE_A))
+		return fail(GRAV_E_ARG, "the single-launch step takes GRAV_S2_INTEGRATE and GRAV_S2_WRITE_A only");
+	if ((flags & GRAV_S2_WRITE_A) && !b->a_out) return fail(GRAV_E_ARG, "GRAV_S2_WRITE_A without a_out");
+	if (b->n_bodies > GRAV_FUSED_MAX_N)
+		return fail(GRAV_E_SIZE, "%lld bodies: the single-launch step takes at most %d",
+			(long long)b->n_bodies, GRAV_FUSED_MAX_N);
+	if (!grav_fused_supported(b->mode, static_cast<int32_t>(b->n_bodies), threads, rows))
+		return fail(GRAV_E_TILE, "no single-launch step for mode %d, %d threads, %d rows", b->mode,
+			threads, rows);
+	if (b->n_bodies == 0) return ok();
+	cudaError_t e = grav::launch_fused(*b, flags, threads, rows, sync,
+		static_cast<cudaStream_t>(stream));
+	if (e != cudaSuccess) return cuda_fail(e, "single-launch step (cooperative launch)");
+	return ok();
+}
+
 int grav_host_device_pointer(const void* host, void** dev)
 {
 	if (!host || !dev) return fail(GRAV_E_ARG, "NULL host or dev pointer");

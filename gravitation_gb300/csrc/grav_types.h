@@ -24,6 +24,12 @@ struct Stage1Kernel {
 cudaError_t launch_stage2(const grav_batch& b, int flags, cudaStream_t stream,
 	bool dependent = true);
 
+// Single-launch step of one small universe (fused.cu).
+const void* find_fused(int mode, int threads);
+cudaError_t launch_fused(const grav_batch& b, int flags, int threads, int rows, int32_t* sync,
+	cudaStream_t stream);
+int fused_occupancy(int mode, int64_t n, int threads, int rows, int* ctas_per_sm);
+
 // Kernel tables, one per translation unit (stage1_f32.cu, stage1_f64.cu).
 int stage1_table_f32(const Stage1Kernel** out);
 int stage1_table_f64(const Stage1Kernel** out);

@@ -184,6 +184,28 @@ def default_tile(mode, sizes, device=None):
     return best[1]
 
 
+FUSED_MODES = ('fp32', 'fp32n', 'fp32c')
+# (largest n, (threads, rows)) of the single-launch step, fastest measured on GB300
+# (graph-replayed steps, fp32n / fp32): n <= 64 -- 5.0-5.3 / 3.9-4.1 us against 8.8 /
+# 7.8 us for the two-launch step; 128 -- 6.2 / 4.7 against 8.8 / 7.9; 256 -- 6.9 / 6.1
+# against 8.9 / 7.8; 512 -- 8.4 / 6.8 against 9.0 / 8.3.  From 1024 bodies on the
+# two-launch step, whose stage 1 spreads the pairs over every SM, is as fast or faster.
+FUSED_RULE = ((64, (256, 64)), (128, (512, 128)), (256, (256, 32)), (512, (512, 32)))
+
+
+def default_fused(mode, sizes, dev_info=None):
+    """(threads, rows) of the single-launch step (grav_step_fused) for this workload, or
+    None for the two-launch step: one universe of at most 512 bodies in an all-pairs
+    FP32 mode."""
+    if len(sizes) != 1 or mode not in FUSED_MODES:
+        return None
+    n = int(sizes[0])
+    for n_max, cfg in FUSED_RULE:
+        if 0 < n <= n_max:
+            return cfg
+    return None
+
+
 class Engine:
     """Packed batch of universes on one GB300 with FP64 state.
 
@@ -194,9 +216,12 @@ class Engine:
               (near pairs from double-single separations), 'fp32c' / 'fp32cu'
               (double-single separations for every pair) or 'fp64'
       tile  : _lib.Tile, or None to use the autotuner's choice / the default shape
+      fused : single-launch step (grav_step_fused) for one small universe: (threads,
+              rows) per CTA, False for the two-launch step, None to decide by size
+              (default_fused)
     """
 
-    def __init__(self, sizes, T, mode='fp32', tile=None, device=None, tuner=None):
+    def __init__(self, sizes, T, mode='fp32', tile=None, device=None, tuner=None, fused=None):
         self.lib = _lib.load()
         self.dev_info = device_info(device)
         self.device = torch.device('cuda', self.dev_info.index)
@@ -257,6 +282,24 @@ class Engine:
         self.batch = b
         self._bref = ctypes.byref(b)
         self.offsets = np.array([u.body_off for u in list(univ)[:info.n_univ]], dtype=np.int64)
+        if fused is None:
+            fused = default_fused(self.mode_name, self.sizes, self.dev_info)
+        self.fused = None
+        if fused:
+            threads, rows = int(fused[0]), int(fused[1])
+            n = self.sizes[0] if len(self.sizes) == 1 else -1
+            if len(self.sizes) != 1 or not self.lib.grav_fused_supported(self.mode, n, threads, rows):
+                raise ValueError('no single-launch step for mode %s, sizes %s, %d threads, %d rows'
+                                 % (self.mode_name, self.sizes[:4], threads, rows))
+            occ = ctypes.c_int32()
+            with torch.cuda.device(dev):
+                check(self.lib.grav_fused_occupancy(self.mode, n, threads, rows, ctypes.byref(occ)))
+            if -(-n // rows) > occ.value * self.dev_info.sm_count:
+                raise ValueError('%d CTAs of the single-launch step are not resident at once'
+                                 % -(-n // rows))
+            self.fused = (threads, rows)
+            # grid-barrier counters of grav_step_fused (zero between calls)
+            self.sync = torch.zeros(2, dtype=torch.int32, device=dev)
 
     # ---- state ----------------------------------------------------------------------
     def set_state(self, r, v, gm, stream=None):
@@ -341,9 +384,16 @@ class Engine:
         check(self.lib.grav_stage2(self._bref, int(flags), self._h(stream)))
 
     def step(self, steps=1, stream=None, write_a=False):
-        """`steps` full steps (stage 1 + stage 2) queued on the stream."""
+        """`steps` full steps (stage 1 + stage 2, or the single-launch step) queued on the
+        stream."""
         flags = _lib.GRAV_S2_INTEGRATE | (_lib.GRAV_S2_WRITE_A if write_a else 0)
         h = self._h(stream)
+        if self.fused:
+            threads, rows = self.fused
+            sync = ctypes.c_void_p(self.sync.data_ptr())
+            for _ in range(int(steps)):
+                check(self.lib.grav_step_fused(self._bref, flags, threads, rows, sync, h))
+            return
         for _ in range(int(steps)):
             check(self.lib.grav_step(self._bref, flags, h))
 

@@ -169,7 +169,7 @@ class Tuner:
         def time_tile(t, min_ms):
             """ms per step of tile t: full steps replayed from a CUDA graph, enough
             replays for about `min_ms` of steps (short steps time noisily)."""
-            eng = Engine(sizes, step_T, mode=mode, tile=t, device=dev_info.index)
+            eng = Engine(sizes, step_T, mode=mode, tile=t, device=dev_info.index, fused=False)
             eng.set_state(r, v, gm)
             s = torch.cuda.current_stream(eng.device)
             g = eng.capture_graph(reps)

@@ -285,7 +285,8 @@ def run_sweep(sizes=None, mode=None, reps=50, tuner=None, device=None):
     the state in HBM.  mode None: the plugin's float32 default at each size (all pairs
     below 8192 bodies, unique pairs from there, near pairs corrected).  Below 8192 bodies
     one graph replay holds 20 steps, so that the host's graph-launch rate does not set
-    the measured step time; above, one step per replay.  At least `reps` steps are
+    the measured step time; above, one step per replay.  Up to 512 bodies the engine
+    takes the single-launch step (grav_step_fused).  At least `reps` steps are
     timed: the near-pair kernels' cost follows the state, which at the reference's time
     step streams from the cube towards the shape of its velocity distribution."""
     from .plugin import default_mode
@@ -315,6 +316,8 @@ def run_sweep(sizes=None, mode=None, reps=50, tuner=None, device=None):
         res.append({'n': n, 'mode': m_n, 'ms_per_step': ms,
                     'interactions_per_s': n * n / (ms * 1e-3),
                     'steps_per_replay': per,
+                    'kernel': ('single launch (threads, rows) = %d, %d' % eng.fused
+                               if eng.fused else 'stage 1 + stage 2'),
                     'tile': [eng.tile.bpt, eng.tile.threads, eng.tile.jtile, eng.info.grid]})
         eng.raise_on_device_error()
     return res

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define GRAV_ABI_VERSION 4
+#define GRAV_ABI_VERSION 5
 
 /* status codes */
 #define GRAV_OK 0
@@ -222,6 +222,41 @@ int grav_stage2(const grav_batch* b, int flags, void* stream);
 /* Stage 1 then stage 2 with `flags` (one full step when GRAV_S2_INTEGRATE).
  * Replaces universe_base.step's stage 1 and stage 2 calls (_base_.py:143-144). */
 int grav_step(const grav_batch* b, int flags, void* stream);
+
+/* ---- single-launch step for one small universe ---------------------------------- */
+
+/* Largest universe grav_step_fused takes (every CTA holds all positions in shared
+ * memory). */
+#define GRAV_FUSED_MAX_N 4096
+
+/* 1 if grav_step_fused has a kernel for `mode` (GRAV_MODE_FP32, GRAV_MODE_FP32C or
+ * GRAV_MODE_FP32N), `threads` per CTA (256, 512 or 1024) and `rows` per CTA
+ * (1 <= rows <= threads) at n bodies (n <= GRAV_FUSED_MAX_N), else 0. */
+int grav_fused_supported(int mode, int32_t n, int32_t threads, int32_t rows);
+
+/* Resident CTAs per SM of that kernel on the current device; grav_step_fused launches
+ * ceil(n / rows) CTAs, which must not exceed SMs x this. */
+int grav_fused_occupancy(int mode, int32_t n, int32_t threads, int32_t rows,
+	int32_t* ctas_per_sm);
+
+/*
+ * One full step (GRAV_S2_INTEGRATE, optionally GRAV_S2_WRITE_A) of a batch holding one
+ * universe (laid out by grav_plan: its rows start at row 0 of r, v and pos, and
+ * b->n_bodies is its size), in a single cooperative launch of ceil(n / rows) CTAs of `threads` threads:
+ * each CTA copies every body's stage-1 position to shared memory, completes the
+ * accelerations of its `rows` rows over all bodies and applies stage 2 to them (the
+ * same pair arithmetic, compensated sums and FP64 update as grav_stage1 + grav_stage2,
+ * summed in another order: results agree to FP32 rounding of the partial sums).  The
+ * writes wait for every CTA's copy on a grid barrier over `sync`, two device int32
+ * that are zero before the first call and that every completed call leaves zero.  The
+ * barrier's wait is bounded: after 2 s it sets GRAV_DEV_TIMEOUT in b->err and
+ * the step writes nothing (zero `sync` again before the next call).  b->part is not
+ * used.  Replaces universe_base.step's stage 1 and stage 2 calls (_base_.py:143-144)
+ * for universes of up to GRAV_FUSED_MAX_N bodies, where launch latency sets the
+ * step's time.
+ */
+int grav_step_fused(const grav_batch* b, int flags, int32_t threads, int32_t rows,
+	int32_t* sync, void* stream);
 
 /* ---- diagnostics -------------------------------------------------------------------- */
 

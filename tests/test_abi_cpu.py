@@ -311,3 +311,42 @@ def test_header_compiles_as_c_and_matches_binding(L, tmp_path):
     assert L.grav_plan(2, n_arr, T_arr, ctypes.byref(t), ctypes.byref(info), None, None) == 0
     assert (nb, nu, nseg, grid) == (info.n_bodies, info.n_univ, info.n_seg, info.grid)
     assert out['bad'] == '1'
+
+
+def test_fused_step_rejects_bad_calls_on_host(L):
+    """grav_step_fused validates on the host (nothing reaches a GPU here)."""
+    f32, f32n, f32c = _lib.GRAV_MODE_FP32, _lib.GRAV_MODE_FP32N, _lib.GRAV_MODE_FP32C
+    for m in (f32, f32n, f32c):
+        for threads in (256, 512, 1024):
+            assert L.grav_fused_supported(m, 100, threads, 32) == 1
+            assert L.grav_fused_supported(m, _lib.GRAV_FUSED_MAX_N, threads, threads) == 1
+            assert L.grav_fused_supported(m, _lib.GRAV_FUSED_MAX_N + 1, threads, 32) == 0
+            assert L.grav_fused_supported(m, 100, threads, threads + 1) == 0
+            assert L.grav_fused_supported(m, 100, threads, 0) == 0
+        assert L.grav_fused_supported(m, 100, 128, 32) == 0
+    for m in (_lib.GRAV_MODE_FP64, _lib.GRAV_MODE_FP32U, _lib.GRAV_MODE_FP32UN,
+              _lib.GRAV_MODE_FP32CU, 99):
+        assert L.grav_fused_supported(m, 100, 256, 32) == 0
+    sync = ctypes.c_void_p(16)   # never dereferenced: validation fails first
+    assert L.grav_step_fused(None, 1, 256, 32, sync, None) == _lib.GRAV_E_ARG
+    b = _lib.Batch()
+    b.mode = f32
+    b.tile = _lib.Tile(1, 128, 128, 1)
+    b.n_seg, b.n_pad_total, b.n_bodies, b.n_univ = 1, 128, 100, 1
+    b.univ = b.seg = b.pos = b.r = b.v = 16
+    b.eps2 = 1e-25
+    bb = ctypes.byref(b)
+    assert L.grav_step_fused(bb, 1, 256, 32, None, None) == _lib.GRAV_E_ARG       # no sync
+    assert L.grav_step_fused(bb, _lib.GRAV_S2_PREPARE, 256, 32, sync, None) == _lib.GRAV_E_ARG
+    assert L.grav_step_fused(bb, _lib.GRAV_S2_WRITE_A, 256, 32, sync, None) == _lib.GRAV_E_ARG
+    assert L.grav_step_fused(bb, 1, 128, 32, sync, None) == _lib.GRAV_E_TILE     # threads
+    assert L.grav_step_fused(bb, 1, 256, 300, sync, None) == _lib.GRAV_E_TILE    # rows
+    b.n_univ = 2
+    assert L.grav_step_fused(bb, 1, 256, 32, sync, None) == _lib.GRAV_E_ARG
+    assert 'one universe' in _lib.last_error()
+    b.n_univ = 1
+    b.mode = _lib.GRAV_MODE_FP32U
+    assert L.grav_step_fused(bb, 1, 256, 32, sync, None) == _lib.GRAV_E_TILE
+    b.mode = f32
+    b.n_seg, b.n_pad_total, b.n_bodies = 33, 33 * 128, _lib.GRAV_FUSED_MAX_N + 1
+    assert L.grav_step_fused(bb, 1, 256, 32, sync, None) == _lib.GRAV_E_SIZE
