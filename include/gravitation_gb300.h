@@ -242,18 +242,19 @@ int grav_fused_occupancy(int mode, int32_t n, int32_t threads, int32_t rows,
 /*
  * One full step (GRAV_S2_INTEGRATE, optionally GRAV_S2_WRITE_A) of a batch holding one
  * universe (laid out by grav_plan: its rows start at row 0 of r, v and pos, and
- * b->n_bodies is its size), in a single cooperative launch of ceil(n / rows) CTAs of `threads` threads:
- * each CTA copies every body's stage-1 position to shared memory, completes the
- * accelerations of its `rows` rows over all bodies and applies stage 2 to them (the
- * same pair arithmetic, compensated sums and FP64 update as grav_stage1 + grav_stage2,
- * summed in another order: results agree to FP32 rounding of the partial sums).  The
- * writes wait for every CTA's copy on a grid barrier over `sync`, two device int32
- * that are zero before the first call and that every completed call leaves zero.  The
- * barrier's wait is bounded: after 2 s it sets GRAV_DEV_TIMEOUT in b->err and
- * the step writes nothing (zero `sync` again before the next call).  b->part is not
- * used.  Replaces universe_base.step's stage 1 and stage 2 calls (_base_.py:143-144)
- * for universes of up to GRAV_FUSED_MAX_N bodies, where launch latency sets the
- * step's time.
+ * b->n_bodies is its size), in a single launch of ceil(n / rows) CTAs of `threads`
+ * threads (one thread-block cluster up to 16 CTAs where the GPU can schedule it, else a
+ * cooperative launch).  Each CTA copies every body's stage-1 position to shared memory,
+ * completes the accelerations of its `rows` rows over all bodies and applies stage 2 to
+ * them: the same pair arithmetic, compensated sums and FP64 update as grav_stage1 +
+ * grav_stage2, summed in another order (results agree to FP32 rounding of the partial
+ * sums).  The writes wait for every CTA's copy: on the cluster barrier, or on a grid
+ * barrier over `sync`, two device int32 that are zero before the first call and that
+ * every completed call leaves zero.  The grid barrier's wait is bounded: after 2 s it
+ * sets GRAV_DEV_TIMEOUT in b->err and the step writes nothing (zero `sync` again before
+ * the next call).  b->part is not used.  Replaces universe_base.step's stage 1 and
+ * stage 2 calls (_base_.py:143-144) for universes of up to GRAV_FUSED_MAX_N bodies,
+ * where launch latency sets the step's time.
  */
 int grav_step_fused(const grav_batch* b, int flags, int32_t threads, int32_t rows,
 	int32_t* sync, void* stream);
