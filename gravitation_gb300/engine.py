@@ -235,8 +235,10 @@ class Engine:
             self.mode_name = {v: k for k, v in _lib.MODES.items()}[self.mode]
         self.sizes = [int(x) for x in sizes]
         self.T = list(T) if np.ndim(T) else [float(T)] * len(self.sizes)
+        if fused is None:
+            fused = default_fused(self.mode_name, self.sizes, self.dev_info)
         if tile is None:
-            if tuner is not None:
+            if tuner is not None and not fused:
                 tile = tuner.choose(self.mode_name, self.sizes, self.dev_info, T=self.T)
             else:
                 tile = default_tile(self.mode_name, self.sizes, self.dev_info.index)
@@ -283,8 +285,6 @@ class Engine:
         self.batch = b
         self._bref = ctypes.byref(b)
         self.offsets = np.array([u.body_off for u in list(univ)[:info.n_univ]], dtype=np.int64)
-        if fused is None:
-            fused = default_fused(self.mode_name, self.sizes, self.dev_info)
         self.fused = None
         if fused:
             threads, rows = int(fused[0]), int(fused[1])

@@ -21,7 +21,9 @@ def lib():
 def test_buckets():
     assert bucket_of([1000]) == 'single:1024'
     assert bucket_of([1024]) == 'single:1024'
-    assert bucket_of([1025]) == 'single:2048'
+    assert bucket_of([1025]) == 'single:1280'
+    assert bucket_of([5000]) == 'single:5120'
+    assert bucket_of([8000]) == 'single:8192'
     a, b = bucket_of([64, 128, 9000]), bucket_of([9000, 64, 128])
     assert a == b == 'batch:u4:w26:max16384'
     # the same make-up shares a key; another make-up does not
@@ -69,3 +71,15 @@ def test_choose_without_tuning_uses_the_cache(tmp_path):
     t.store('fp32u', [65536], DEV, _lib.Tile(8, 128, 256, 456), 1.3)
     got = t.choose('fp32u', [65536], DEV, tune_if_missing=False)
     assert (got.bpt, got.threads, got.jtile, got.grid) == (8, 128, 256, 456)
+
+
+def test_quarter_octave_classes():
+    from gravitation_gb300.tune import fine_class
+    assert [fine_class(n) for n in (0, 1, 3, 4, 5, 8, 9, 11, 13, 16, 17)] == \
+        [0, 1, 3, 4, 5, 8, 10, 12, 14, 16, 20]
+    assert [fine_class(n) for n in (4097, 5000, 5121, 6144, 6145, 7169, 8192)] == \
+        [5120, 5120, 6144, 6144, 7168, 8192, 8192]
+    for n in range(4, 70000, 37):
+        c = fine_class(n)
+        assert n <= c < 1.26 * n + 1, n
+        assert fine_class(c) == c
