@@ -44,19 +44,21 @@ def default_adjoint_pairs(sizes, budget=None):
 
 
 def default_adjoint_tile(sizes, pairs=False):
-    """Tile of the backward pair kernel.  All pairs: up to ~10k bodies (1e8 ordered pairs) a step is
-    latency bound and one body per thread (the finest work units) is fastest; above,
+    """Tile of the backward pair kernel.  Unique pairs: 2 rows/thread, 8 warps and
+    64-body j-tiles up to ~20k bodies, 4 rows/thread (compensated sums in shared memory),
+    4 warps and 128-body j-tiles above.  Measured on GB300, backward step with the
+    accelerations recomputed / kept, tiles 2/256/64, 2/128/64, 4/128/128: N = 8192 --
+    85 / 71, 84 / 69, 81 / 70 us; N = 16384 -- 274 / 232, 283 / 235, 289 / 254 us;
+    N = 32768 -- 1035 / 871, 1091 / 895, 967 / 854 us; N = 65536 -- 4.08 / 3.43,
+    4.28 / 3.52, 3.77 / 3.33 ms.  All pairs: up to ~10k bodies (1e8 ordered pairs) a step
+    is latency bound and one body per thread (the finest work units) is fastest; above,
     two bodies per thread.  Measured on GB300, backward step: N = 4096 -- 37.8 us with
     (1, 128, 128), 40.4 us with (2, 128, 128), 37.9 / 40.3 / 43.3 / 48.8 us with
     (1, 64, 128) / (2, 64, 128) / (1, 128, 64) / (2, 64, 64); N = 65536 -- 5.16 ms with
     (2, 128, 128), 5.62 ms with (1, 128, 128)."""
     if pairs:
-        # unique pairs: 2 rows/thread and 64-body j-tiles (8 warps up to ~6k bodies, 4
-        # warps up to ~20k), 4 rows/thread and 128-body j-tiles above
         n2 = sum(int(n) * int(n) for n in sizes)
-        if n2 < 40_000_000:
-            return (2, 256, 64)
-        return (2, 128, 64) if n2 <= 400_000_000 else (4, 128, 128)
+        return (2, 256, 64) if n2 <= 400_000_000 else (4, 128, 128)
     if sum(int(n) * int(n) for n in sizes) <= 100_000_000:
         return (1, 128, 128)
     return ADJ_TILE

@@ -24,6 +24,10 @@
 // as FP32, to the column slot of (I, J) (block J's last J slots).  Row
 // sums are compensated FP32 (TwoSum) and go out as FP32 (hi, lo) pairs.  Slot layout
 // [slot][NC][R]: a, h, g (NC = 7) or h, g (NC = 4).
+#include <mutex>
+#include <set>
+#include <utility>
+
 #include "grav_device.cuh"
 
 namespace grav {
@@ -48,6 +52,11 @@ __global__ void __launch_bounds__(32 * W) vjp_sym_kernel(const grav_batch b,
 	// at the flush (no shared-memory atomics, whose order would depend on warp timing)
 	__shared__ float colacc[W][NC][JT];
 	__shared__ __align__(8) uint64_t bar[2];
+	// with 4 rows per thread the compensated row sums (hi, lo) live in shared memory,
+	// touched once per j-tile, instead of 20 registers per row: 128 instead of 168
+	// registers with the accelerations recomputed, a fourth resident CTA per SM
+	constexpr bool SS = B >= 4;
+	__shared__ float2 csum[SS ? NC : 1][SS ? B : 1][SS ? T : 1];
 
 	const int tid = threadIdx.x;
 	const int lane = tid & 31;
@@ -117,6 +126,10 @@ __global__ void __launch_bounds__(32 * W) vjp_sym_kernel(const grav_batch b,
 				ah[q3][k] = al[q3][k] = hh[q3][k] = hl[q3][k] = 0.f;
 			}
 			fs[k] = fg[k] = gh[k] = gl[k] = 0.f;
+			if (SS) {
+#pragma unroll
+				for (int q = 0; q < NC; ++q) csum[SS ? q : 0][SS ? k : 0][SS ? tid : 0] = make_float2(0.f, 0.f);
+			}
 		}
 
 		for (int t = 0; t < nt; ++t, ++gt) {
@@ -265,13 +278,30 @@ __global__ void __launch_bounds__(32 * W) vjp_sym_kernel(const grav_batch b,
 				const float ui[3] = {uxi[k], uyi[k], uzi[k]};
 #pragma unroll
 				for (int q3 = 0; q3 < 3; ++q3) {
-					if constexpr (FA) two_sum_acc(ah[q3][k], al[q3][k], fa[q3][k]);
 					// h = Gm_i P - u_i S - 3 Q
 					const float ht = fmaf(gi[k], fp[q3][k], fmaf(-ui[q3], fs[k], -3.f * fq[q3][k]));
-					two_sum_acc(hh[q3][k], hl[q3][k], ht);
+					if (SS) {
+						if constexpr (FA) {
+							float2 v = csum[SS ? q3 : 0][SS ? k : 0][SS ? tid : 0];
+							two_sum_acc(v.x, v.y, fa[q3][k]);
+							csum[SS ? q3 : 0][SS ? k : 0][SS ? tid : 0] = v;
+						}
+						float2 v = csum[SS ? H0 + q3 : 0][SS ? k : 0][SS ? tid : 0];
+						two_sum_acc(v.x, v.y, ht);
+						csum[SS ? H0 + q3 : 0][SS ? k : 0][SS ? tid : 0] = v;
+					} else {
+						if constexpr (FA) two_sum_acc(ah[q3][k], al[q3][k], fa[q3][k]);
+						two_sum_acc(hh[q3][k], hl[q3][k], ht);
+					}
 					fa[q3][k] = fp[q3][k] = fq[q3][k] = 0.f;
 				}
-				two_sum_acc(gh[k], gl[k], fg[k]);
+				if (SS) {
+					float2 v = csum[SS ? G0 : 0][SS ? k : 0][SS ? tid : 0];
+					two_sum_acc(v.x, v.y, fg[k]);
+					csum[SS ? G0 : 0][SS ? k : 0][SS ? tid : 0] = v;
+				} else {
+					two_sum_acc(gh[k], gl[k], fg[k]);
+				}
 				fs[k] = fg[k] = 0.f;
 			}
 		}
@@ -285,11 +315,17 @@ __global__ void __launch_bounds__(32 * W) vjp_sym_kernel(const grav_batch b,
 		for (int k = 0; k < B; ++k) {
 			const int i = r0 + k * 32;
 #pragma unroll
-			for (int q3 = 0; q3 < 3; ++q3) {
-				if constexpr (FA) out[q3 * R + i] = make_float2(ah[q3][k], al[q3][k]);
-				out[(H0 + q3) * R + i] = make_float2(hh[q3][k], hl[q3][k]);
+			if (SS) {
+#pragma unroll
+				for (int q = 0; q < NC; ++q) out[q * R + i] = csum[SS ? q : 0][SS ? k : 0][SS ? tid : 0];
+			} else {
+#pragma unroll
+				for (int q3 = 0; q3 < 3; ++q3) {
+					if constexpr (FA) out[q3 * R + i] = make_float2(ah[q3][k], al[q3][k]);
+					out[(H0 + q3) * R + i] = make_float2(hh[q3][k], hl[q3][k]);
+				}
+				out[G0 * R + i] = make_float2(gh[k], gl[k]);
 			}
-			out[G0 * R + i] = make_float2(gh[k], gl[k]);
 		}
 		ub = S.unit_begin + t1;
 		++s;
@@ -334,10 +370,28 @@ const VjpSymKernel* find_vjp_sym(int bpt, int threads, int jtile, bool fa)
 // Launch the unique-pair backward pair kernel (programmatic dependent; it waits with
 // grid_dep_wait before it reads); fa: recompute the accelerations (7 slot components)
 // or not (4).  Returns cudaErrorInvalidValue for a shape that is not compiled.
+// Raise the kernel's dynamic shared-memory limit to its launch size (static plus dynamic
+// above 48 KB needs the opt-in: the 4-rows-per-thread shapes), once per kernel and device.
+static cudaError_t ensure_vjp_smem(const VjpSymKernel* k)
+{
+	static std::mutex mu;
+	static std::set<std::pair<int, const void*>> done;
+	int dev = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if (e != cudaSuccess) return e;
+	std::lock_guard<std::mutex> lock(mu);
+	if (done.count({dev, k->fn})) return cudaSuccess;
+	e = cudaFuncSetAttribute(k->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, k->smem);
+	if (e == cudaSuccess) done.insert({dev, k->fn});
+	return e;
+}
+
 cudaError_t launch_vjp_sym(const grav_batch& b, const float4* upos, bool fa, cudaStream_t st)
 {
 	const VjpSymKernel* k = find_vjp_sym(b.tile.bpt, b.tile.threads, b.tile.jtile, fa);
 	if (!k) return cudaErrorInvalidValue;
+	cudaError_t e = ensure_vjp_smem(k);
+	if (e != cudaSuccess) return e;
 	grav_batch copy = b;
 	void* args[] = {&copy, &upos};
 	return launch_dependent(k->fn, b.tile.grid, k->threads, k->smem, st, args);
@@ -351,8 +405,9 @@ int vjp_sym_occupancy(int bpt, int threads, int jtile, int* ctas_per_sm)
 		const VjpSymKernel* k = find_vjp_sym(bpt, threads, jtile, fa);
 		if (!k) return 0;
 		int occ = 0;
-		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k->fn, k->threads, k->smem) !=
-			cudaSuccess)
+		if (ensure_vjp_smem(k) != cudaSuccess ||
+			cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k->fn, k->threads, k->smem) !=
+				cudaSuccess)
 			return -1;
 		best = best < 0 ? occ : min(best, occ);
 	}

@@ -67,6 +67,32 @@ def test_single_step_against_oracle_vjp(gpu, pairs, store_a):
     assert np.max(np.abs(v_rev.cpu().numpy() - v)) <= 1e-15 + 1e-9 * np.max(np.abs(v))
 
 
+@pytest.mark.parametrize('tile', [(2, 256, 64), (2, 128, 64), (4, 128, 128)])
+@pytest.mark.parametrize('store_a', [False, True])
+def test_single_step_every_unique_pair_tile(gpu, tile, store_a):
+    """Every compiled shape of the unique-pair backward kernel (2 rows per thread with the
+    compensated sums in registers, 4 with them in shared memory), with and without the
+    forward's accelerations, against the oracle's VJP: 1500 bodies, 3 row blocks of 512
+    rows at 4 rows per thread, so that column slots are used."""
+    from gravitation_gb300.adjoint import AdjointEngine
+    n = 1500
+    r, v, m = compact(n, 5)
+    c = np.random.default_rng(6).normal(size=(n, 3))
+    ro = Rollout([n], T, 1, every=1, store_a=store_a, mode='fp32')
+    ro.adj = AdjointEngine([n], T, tile=tile, pairs=True)
+    dev = torch.device('cuda')
+    ro.forward(torch.tensor(r, device=dev), torch.tensor(v, device=dev),
+               torch.tensor(G_DEFAULT * m, device=dev))
+    gr, gv, ggm = ro.backward(torch.tensor(c, device=dev),
+                              torch.zeros((n, 3), device=dev, dtype=torch.float64))
+    ro.adj.raise_on_device_error()
+    h, g = oracle.vjp_fp64(r, m, G_DEFAULT, T * c)
+    assert relerr(gr.cpu().numpy(), c + T * h) < 1e-6
+    assert relerr(ggm.cpu().numpy(), -T * g) < 1e-5
+    r_rev, _ = ro.reversed_state
+    assert np.max(np.abs(r_rev.cpu().numpy() - r)) <= 1e-12 * np.max(np.abs(r))
+
+
 @pytest.mark.parametrize('store_a', [False, True])
 def test_single_step_batch_one_lane_per_row(gpu, store_a):
     """A batch of two universes with more than 16384 padded rows, where the adjoint stage

@@ -165,3 +165,24 @@ def test_graph_step_matches_launched_step(gpu, sync):
     for rv in out[1:]:
         assert np.array_equal(out[0][0], rv[0]) and np.array_equal(out[0][1], rv[1])
     assert not np.array_equal(out[0][0], r)
+
+
+def test_plugin_small_universe_single_launch(gpu):
+    """A small universe through the plugin takes the single-launch step, with the state
+    in the pinned host mirror (read and written in place by the kernel) and the step
+    replayed from a CUDA graph: the trajectory is the FP64 oracle's to the rounding of
+    the FP32 forces, and pm._r / pm._v follow every step."""
+    n = 300
+    r0, v0, m = uniform_cube(n, seed=4)
+    u = make_universe(r0, v0, m, dtype='float32')
+    assert u._gb.fused and u._gb_zero_copy and u._gb_graph is not None
+    for k in range(1, 6):
+        u.step()
+        r, v = state(u)
+        r64, v64 = oracle.rollout_fp64(r0, v0, m, G_DEFAULT, 1e3, k)
+        # per body: |r - r64| / |r64| (a coordinate near zero would inflate a
+        # per-component ratio)
+        err = np.linalg.norm(r - r64, axis=1) / np.linalg.norm(r64, axis=1)
+        assert err.max() < 1e-12, (k, err.max())
+        assert np.max(np.abs(v - v64)) < 1e-9, k
+    u.stop()
