@@ -350,3 +350,24 @@ def test_fused_step_rejects_bad_calls_on_host(L):
     b.mode = f32
     b.n_seg, b.n_pad_total, b.n_bodies = 33, 33 * 128, _lib.GRAV_FUSED_MAX_N + 1
     assert L.grav_step_fused(bb, 1, 256, 32, sync, None) == _lib.GRAV_E_SIZE
+
+
+def test_eps2_is_not_a_softening_length_for_the_scenarios(L):
+    """The r^2 floor grows with the heaviest G*m (it keeps G*m * r^-3 finite in FP32 at
+    zero separation); for the reference's own scenarios, scaled as the universe scales
+    them, sqrt(eps2) stays at least 1e6 below the closest pair's separation, so no pair
+    term is softened: the galaxy (a 4e40 kg hole among 2e30 kg stars, scale_r 1e-10,
+    scale_m 1e-30) and the uniform cube and Plummer pair at their SI scale."""
+    from gravitation_gb300.scenarios import G_DEFAULT, galaxy, plummer_pair, uniform_cube
+    r, _, m, p = galaxy(2048, seed=3)
+    Gs = G_DEFAULT * p['scale_r'] ** 3 / p['scale_m']
+    cases = [(r * p['scale_r'], Gs * m * p['scale_m'])]
+    r, _, m = uniform_cube(2048, seed=0)
+    cases.append((r, G_DEFAULT * m))
+    r, _, m = plummer_pair(2048, seed=2)
+    cases.append((r, G_DEFAULT * m))
+    for r, gm in cases:
+        eps2 = L.grav_eps2(float(gm.max()))
+        d2 = ((r[:, None, :] - r[None, :, :]) ** 2).sum(-1)
+        np.fill_diagonal(d2, np.inf)
+        assert np.sqrt(eps2) < 1e-6 * np.sqrt(d2.min()), (eps2, d2.min())
