@@ -29,8 +29,10 @@ Kernel options (keyword arguments of the constructor, kept in self._meta):
   host_sync  'full' (upload + download every step) | 'pull' (download only) |
              'none' (device state only; call sync_host() to refresh the mirror)
   fuse       True (default): stage 1 and stage 2 both run in step_stage1 on the GPU
-             and step_stage2 refreshes the mirror; False: step_stage1 fills pm._a
-             like the reference's kernels and step_stage2 integrates on the GPU
+             (for one universe of up to 512 bodies in a single kernel, the engine's
+             single-launch step) and step_stage2 refreshes the mirror; False:
+             step_stage1 fills pm._a like the reference's kernels and step_stage2
+             integrates on the GPU
   tile       (bpt, threads, jtile) to force a tile shape; default: autotuned
   autotune   True (default) to use the autotuner cache / tuning
   device     CUDA device index (default: current device)
