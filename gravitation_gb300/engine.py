@@ -187,9 +187,9 @@ def default_tile(mode, sizes, device=None):
 FUSED_MODES = ('fp32', 'fp32n', 'fp32c')
 # (largest n, (threads, rows)) of the single-launch step, the fastest measured on GB300
 # (graph-replayed steps, fp32n / fp32, against the two-launch step's 8.7-9.0 / 7.7-8.3
-# us): n <= 32 -- 3.8-3.9 / 3.5-3.6 us (one CTA); 64 -- 4.6 / 4.0 (one CTA); 128 -- 5.2 /
-# 4.5 (a cluster of 4 CTAs); 256 -- 5.8 / 5.2 (8); 512 -- 7.0 / 5.9 (16).  From 1024 bodies
-# the two-launch step, whose stage 1 spreads the pairs over every SM, is faster (9.3 us
+# us): n <= 32 -- 3.6 / 3.5 us (one CTA); 64 -- 4.2 / 4.0 (one CTA); 128 -- 4.8 / 4.5 (a
+# cluster of 4 CTAs); 256 -- 5.3 / 5.2 (8); 512 -- 6.5 / 5.9 (16).  From 1024 bodies
+# the two-launch step, whose stage 1 spreads the pairs over every SM, is faster (9.4 us
 # against 9.9 at 1024, 10.2 against 13.6 at 2048).
 FUSED_RULE = ((32, (256, 64)), (64, (512, 64)), (128, (256, 32)), (512, (512, 32)))
 
