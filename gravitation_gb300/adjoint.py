@@ -176,7 +176,7 @@ class Rollout:
         self.every = max(1, int(every))
         if mode is None:
             # the forward's FP32 kernel by size, as the plugin picks it: all pairs for
-            # small universes, unique pairs from 8192 bodies while the batch's slots fit,
+            # small universes, unique pairs from 4608 bodies while the batch's slots fit,
             # near pairs from double-single separations.  A final-state loss against a
             # nearby target is ill-conditioned (at the differentiable-rollout workload
             # r_K - t is ~1e-9 of r_K), so the forward's force error reaches the

@@ -387,6 +387,7 @@ static const Stage1Kernel k_table_sym[] = {
 	GRAV_SYM_ENTRY(8, 8, 256),
 	GRAV_SYM_ENTRY(8, 4, 128),
 	GRAV_SYM_ENTRY(8, 4, 64),
+	GRAV_SYM_ENTRY(4, 2, 64),
 	GRAV_SYMC_ENTRY(4, 4, 128),
 	GRAV_SYMC_ENTRY(8, 4, 256),
 	GRAV_SYMC_ENTRY(4, 4, 256),
@@ -397,6 +398,7 @@ static const Stage1Kernel k_table_sym[] = {
 	GRAV_SYMN_ENTRY(8, 4, 64),
 	GRAV_SYMN_ENTRY(4, 4, 256),
 	GRAV_SYMN_ENTRY(4, 8, 256),
+	GRAV_SYMN_ENTRY(4, 2, 64),
 };
 
 int stage1_table_sym(const Stage1Kernel** out)

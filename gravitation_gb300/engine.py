@@ -132,15 +132,24 @@ def slot_budget_bytes(device=None):
     return int(torch.cuda.get_device_properties(idx).total_memory * SLOT_BUDGET_FRACTION)
 
 
-def pair_plan_fits(sizes, budget=None, mode='fp32u', comps=3, tiles=None):
-    """True when the unique-pair plan's slots stay within `budget` bytes (default
-    slot_budget_bytes()) for every shape in `tiles` (default: every compiled shape of
-    `mode`, so that whatever the autotuner picks fits)."""
+def fitting_tiles(sizes, mode, budget=None, comps=3, tiles=None):
+    """The shapes in `tiles` (default: every compiled shape of `mode`) whose plan keeps
+    its partial-sum slots within `budget` bytes (default slot_budget_bytes()); every shape
+    in the all-pairs modes, whose slots do not grow with N^2.  The autotuner and the
+    default shape choose among these."""
+    tiles = list(tile_list(mode) if tiles is None else tiles)
+    if mode not in _lib.PAIR_MODES:
+        return tiles
     if budget is None:
         budget = slot_budget_bytes()
-    if tiles is None:
-        tiles = tile_list(mode)
-    return all(plan_part_bytes(sizes, t, mode, comps) <= budget for t in tiles)
+    return [t for t in tiles if plan_part_bytes(sizes, t, mode, comps) <= budget]
+
+
+def pair_plan_fits(sizes, budget=None, mode='fp32u', comps=3, tiles=None):
+    """True when some shape in `tiles` (default: every compiled shape of `mode`) keeps the
+    unique-pair plan's slots within `budget` bytes (default slot_budget_bytes()); the
+    autotuner and the default shape then pick only such shapes (fitting_tiles)."""
+    return len(fitting_tiles(sizes, mode, budget, comps, tiles)) > 0
 
 
 def _ctypes_to_device(arr, nbytes, device):
@@ -156,7 +165,7 @@ def default_tile(mode, sizes, device=None):
     """Tile shape used when no tuned entry exists: the largest i-tile that still gives
     every resident CTA several work units."""
     info = device_info(device)
-    cands = tile_list(mode)
+    cands = fitting_tiles(sizes, mode) or tile_list(mode)
     best = None
     for t in cands:
         occ = occupancy(mode, t, device)

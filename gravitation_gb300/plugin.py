@@ -17,7 +17,7 @@ Behaviour seen from the front end (README.md:50, worker.py:119-136):
 
 Kernel options (keyword arguments of the constructor, kept in self._meta):
   precision  'fp32n' | 'fp32un' | 'fp32' | 'fp32u' | 'fp32c' | 'fp32cu' | 'fp64'   default
-             from dtype: 'float32' -> fp32n below 8192 bodies, fp32un from there on while
+             from dtype: 'float32' -> fp32n below 4608 bodies, fp32un from there on while
              its partial-sum slots fit an eighth of the GPU's memory (~1.7 M bodies);
              fp32c / fp32cu instead when more than 1e-3 of sampled pairs are near
              (default_mode, near_pair_fraction: discs, dense clusters far out);
@@ -58,11 +58,13 @@ from . import _lib, generate
 from .engine import Engine
 
 # float32 runs the FP32 arithmetic with near pairs corrected, either on unique pairs
-# (fp32un: each pair once, like the reference's CPU kernels; faster from ~8k bodies on)
-# or on all ordered pairs (fp32n: finer work units, faster for small universes); the
-# results agree to FP32 rounding
+# (fp32un: each pair once, like the reference's CPU kernels) or on all ordered pairs
+# (fp32n: finer work units, faster for small universes); the results agree to FP32
+# rounding.  Measured on GB300 (graph-replayed steps on an evolved cube, each mode with
+# its tuned tile), fp32n against fp32un: 3072 bodies 12.9 / 17.1 us, 4096 17.8 / 18.6,
+# 4608 21.3 / 21.4, 6144 30.0 / 25.5, 8192 49.4 / 39.1, 16384 156 / 118.
 _DTYPE_MODE = {'float32': 'fp32n', 'float64': 'fp64'}
-UNIQUE_PAIRS_FROM_N = 8192
+UNIQUE_PAIRS_FROM_N = 4608
 
 
 # Above this fraction of near pairs the near-corrected kernels spend more time on their

@@ -167,7 +167,7 @@ class Tuner:
         distribution, where more pairs are near than in the cube (at T = 1 nothing
         moves, and the tiles with 8 rows per thread timed 12 % faster than they run)."""
         import torch
-        from .engine import Engine, make_plan, occupancy, tile_list
+        from .engine import Engine, fitting_tiles, make_plan, occupancy, tile_list
         from .scenarios import uniform_cube
         sizes = [int(s) for s in sizes]
         rs, vs, ms = [], [], []
@@ -212,7 +212,9 @@ class Tuner:
             return out
 
         timed = []
-        for cand in tile_list(mode):
+        # unique-pair shapes whose partial-sum slots exceed the slot budget at these
+        # sizes are not candidates (rows per block set the slots' N^2 / R growth)
+        for cand in fitting_tiles(sizes, mode) or tile_list(mode):
             occ = occupancy(mode, cand, dev_info.index)
             if occ <= 0:
                 continue

@@ -283,7 +283,7 @@ def run_precision(n=16384, steps=10000, every=100, seed=2,
 def run_sweep(sizes=None, mode=None, reps=50, tuner=None, device=None):
     """Interactions/s of the single-universe step over an N sweep (2^4 .. 2^17), with
     the state in HBM.  mode None: the plugin's float32 default at each size (all pairs
-    below 8192 bodies, unique pairs from there, near pairs corrected).  Below 8192 bodies
+    below 4608 bodies, unique pairs from there, near pairs corrected).  Below 8192 bodies
     one graph replay holds 20 steps, so that the host's graph-launch rate does not set
     the measured step time; above, one step per replay.  Up to 512 bodies the engine
     takes the single-launch step (grav_step_fused).  At least `reps` steps are
@@ -368,7 +368,7 @@ def run_batched(steps=100, warmup=3, mode='fp32un', n_univ=256, seed=1, loop_ste
 
     The batch runs in `mode` with the tile the autotuner picks for the batch.  The loop
     is timed twice: with every universe in the mode and tile the plugin itself would
-    use for it alone (plugin.default_mode: all pairs below 8192 bodies, unique pairs
+    use for it alone (plugin.default_mode: all pairs below 4608 bodies, unique pairs
     from there; each universe's own tuned tile) -- the fair comparison, reported as
     speedup_vs_loop / speedup_vs_graphed_loop -- and with every universe in the batch's
     mode (each its own tuned tile)."""
@@ -529,7 +529,7 @@ def run_frontend(b_min=10, b_max=17, min_iterations=10, min_total_runtime=1.0, s
     and reports the best step time.  Here the universes start from the galaxy generated
     on the device (the reference's generator is unseeded Python) with the recipe's
     universe parameters; dtype float32 as in the scenario, so the plugin picks all pairs
-    below 8192 bodies and unique pairs above."""
+    below 4608 bodies and unique pairs above."""
     import gc
     from . import generate as gen
     from .kernel import gb1

@@ -172,8 +172,8 @@ def fp64_forces_gpu(r, m):
 @pytest.mark.parametrize('mode,n,seed', [('fp32un', 65536, 0), ('fp32n', 8192, 0),
                                          ('fp32n', 4096, 3), ('fp32un', 16384, 1)])
 def test_default_float32_every_body_fp64_state(gpu, mode, n, seed):
-    """The plugin's float32 default (fp32n below 8192 bodies, fp32un from there) on the
-    FP64 state itself: every body within 1e-5 of the FP64 forces (bodies of the uniform
+    """The float32 near-corrected modes (the plugin default: fp32n below 4608 bodies,
+    fp32un from there; fp32n also at 8192) on the FP64 state itself: every body within 1e-5 of the FP64 forces (bodies of the uniform
     cube sit up to 1000 from the origin, where rounding a coordinate to FP32 moves it by
     up to 3e-5: the plain FP32 modes exceed 1e-5 on ~0.2 % of the bodies there)."""
     r, v, m = uniform_cube(n, seed=seed)

@@ -131,7 +131,7 @@ def test_frontend_protocol_workload(gpu):
     assert [r['n'] for r in out['sizes']] == [64, 128, 256, 512]
     for r in out['sizes']:
         assert r['steps'] >= 3 and 0 < r['best_ns'] <= r['avg_ns']
-        # the float32 default below 8192 bodies: near pairs corrected, or double-single
+        # the float32 default below 4608 bodies: near pairs corrected, or double-single
         # separations for every pair where near pairs are common (the galaxy's disc)
         assert r['mode'] in ('fp32n', 'fp32c')
 

@@ -197,10 +197,19 @@ def test_default_precision_by_dtype_and_size():
     assert plan_part_bytes([1 << 20], t, 'fp32') < 64 * 10 ** 6
     assert plan_part_bytes([1 << 22], t, 'fp32u') > 15 * plan_part_bytes([1 << 20], t, 'fp32u')
     assert plan_part_bytes([4096], t, 'fp32u', comps=7) * 3 == plan_part_bytes([4096], t, 'fp32u') * 7
-    # beyond the slot budget float32 falls back to all pairs (forward and backward)
-    worst = max(plan_part_bytes([1 << 20], x, 'fp32un') for x in tile_list('fp32un'))
-    assert default_mode('float32', 1 << 20, budget=worst) == 'fp32un'
-    assert default_mode('float32', 1 << 20, budget=worst - 1) == 'fp32n'
+    # beyond the slot budget float32 falls back to all pairs (forward and backward);
+    # unique pairs stay while some compiled shape fits, and only those are candidates
+    from gravitation_gb300.engine import fitting_tiles
+    sizes = [1 << 20]
+    per_tile = [plan_part_bytes(sizes, x, 'fp32un') for x in tile_list('fp32un')]
+    best, worst = min(per_tile), max(per_tile)
+    assert best < worst        # rows per block set the slots' N^2 / R growth
+    assert default_mode('float32', 1 << 20, budget=best) == 'fp32un'
+    assert default_mode('float32', 1 << 20, budget=best - 1) == 'fp32n'
+    fit = fitting_tiles(sizes, 'fp32un', budget=best)
+    assert fit and all(plan_part_bytes(sizes, x, 'fp32un') <= best for x in fit)
+    assert len(fitting_tiles(sizes, 'fp32un', budget=worst)) == len(per_tile)
+    assert len(fitting_tiles(sizes, 'fp32n', budget=1)) == len(tile_list('fp32n'))
     assert default_mode('float32', 1 << 23, budget=32 * gib) == 'fp32n'
     assert default_adjoint_pairs([4096], budget=32 * gib)
     assert not default_adjoint_pairs([4096], budget=1)
