@@ -2,26 +2,28 @@
 //
 // Below a few thousand bodies a step costs little arithmetic, and the two dependent
 // launches of the regular path (the persistent stage-1 grid, then stage 2 summing its
-// partial-sum slots) set its time: ~8 us at 16-256 bodies on GB300, nearly all launch
-// and drain latency.  Here each CTA copies every body's FP32 position (and low part) into
-// shared memory, completes the accelerations of its own R rows over all columns (no
-// partial sums leave the CTA), and integrates those rows in FP64 exactly as stage2.cu
-// does.  Rows' results are only written after every CTA has finished reading the
-// positions: a grid barrier (arrive right after the copy, wait right before the
-// writes, so it normally costs nothing) on two device counters that the last CTA to
-// leave resets.  The launch is cooperative, so all CTAs are resident together and the
-// barrier always completes; its wait is bounded all the same (GRAV_WAIT_NS), after
-// which the CTA records GRAV_DEV_TIMEOUT, writes nothing and returns.
+// partial-sum slots) set its time: ~8-9 us at 16-512 bodies on GB300, nearly all launch,
+// drain and memory latency.  Here each CTA copies every body's FP32 position (and low
+// part) into shared memory, completes the accelerations of its own R rows over all
+// columns (no partial sums leave the CTA), and integrates those rows in FP64 exactly as
+// stage2.cu does.  A row's results are only written once every CTA has finished reading
+// the positions.  One CTA needs nothing more than its own __syncthreads.  A grid of up to
+// 16 CTAs is one thread-block cluster and uses the hardware cluster barrier (arrive right
+// after the copy, wait right before the writes, so it normally costs nothing).  A larger
+// grid is a cooperative launch, so all its CTAs are resident together, and uses a grid
+// barrier on two device counters that the last CTA to leave resets; its wait is bounded
+// all the same (GRAV_WAIT_NS), after which the CTA records GRAV_DEV_TIMEOUT, writes
+// nothing and returns.
 //
 // Work inside a CTA: warps take items (32-row group g, column split s) of the rows it
-// holds; the columns are cut into as many splits as leave every warp an item, so that
-// few rows still keep all warps busy on short column ranges.  Each lane holds one row; the pair terms
-// are those of stage1_f32.cu (FP32 separations, rsqrt on the SFU, r2 floored by eps2;
-// GRAV_MODE_FP32C: double-single separations; GRAV_MODE_FP32N: pairs closer than the
-// near radius evaluated again from the double-single separation) and every 32 columns
-// the FP32 partials are folded into compensated (TwoSum) sums.  The splits' (hi, lo)
-// sums go through shared memory and are combined in a fixed pairwise tree: the result
-// does not depend on scheduling.
+// holds; the columns are cut into as many splits as leave every warp an item, so that a
+// few rows still keep all warps busy, each on a short column range.  Each lane holds one
+// row; the pair terms are those of stage1_f32.cu (FP32 separations, rsqrt on the SFU, r2
+// floored by eps2; GRAV_MODE_FP32C: double-single separations; GRAV_MODE_FP32N: pairs
+// closer than the near radius evaluated again from the double-single separation) and
+// every 32 columns the FP32 partials are folded into compensated (TwoSum) sums.  The
+// splits' (hi, lo) sums go through shared memory and are combined in a fixed pairwise
+// tree: the result does not depend on scheduling.
 #include "grav_device.cuh"
 
 namespace grav {
