@@ -374,9 +374,12 @@ __global__ void __launch_bounds__(32 * W) stage1_sym_kernel(const grav_batch b)
 #define GRAV_SYMC_ENTRY(B, W, J) \
 	{GRAV_MODE_FP32CU, B, 32 * W, J, \
 		reinterpret_cast<const void*>(&stage1_sym_kernel<B, W, J, 4, SYM_DS>), 2 * 2 * J * 16, false}
+// the near kernel's step loop is not unrolled: with its vote and cold path in every step
+// the unrolled form held 167 registers against 147 and ran 1.4 % slower (N = 65536,
+// tile 8/128/256: stage 1 1.458 against 1.438 ms; unrolled by 2 1.456, by 8 it spilled)
 #define GRAV_SYMN_ENTRY(B, W, J) \
 	{GRAV_MODE_FP32UN, B, 32 * W, J, \
-		reinterpret_cast<const void*>(&stage1_sym_kernel<B, W, J, 4, SYM_NEAR>), 2 * 2 * J * 16, false}
+		reinterpret_cast<const void*>(&stage1_sym_kernel<B, W, J, 1, SYM_NEAR>), 2 * 2 * J * 16, false}
 
 static const Stage1Kernel k_table_sym[] = {
 	GRAV_SYM_ENTRY(4, 4, 128),
