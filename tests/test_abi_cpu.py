@@ -371,3 +371,23 @@ def test_eps2_is_not_a_softening_length_for_the_scenarios(L):
         d2 = ((r[:, None, :] - r[None, :, :]) ** 2).sum(-1)
         np.fill_diagonal(d2, np.inf)
         assert np.sqrt(eps2) < 1e-6 * np.sqrt(d2.min()), (eps2, d2.min())
+
+
+def test_single_launch_rule_names_compiled_kernels(L):
+    """The engine's size rule for the single-launch step only names compiled (mode,
+    threads, rows) combinations, covers one universe of 1-512 bodies in the all-pairs
+    FP32 modes, and nothing else."""
+    from gravitation_gb300.engine import FUSED_MODES, default_fused
+    for mode in FUSED_MODES:
+        m = _lib.MODES[mode]
+        for n in list(range(1, 65)) + [100, 127, 128, 129, 300, 511, 512]:
+            cfg = default_fused(mode, [n])
+            assert cfg is not None, (mode, n)
+            threads, rows = cfg
+            assert L.grav_fused_supported(m, n, threads, rows) == 1, (mode, n, cfg)
+            assert -(-n // rows) <= 16        # one CTA or one thread-block cluster
+        assert default_fused(mode, [513]) is None
+        assert default_fused(mode, [0]) is None
+        assert default_fused(mode, [100, 100]) is None
+    for mode in ('fp32u', 'fp32un', 'fp32cu', 'fp64'):
+        assert default_fused(mode, [100]) is None
