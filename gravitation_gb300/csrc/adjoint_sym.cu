@@ -190,7 +190,9 @@ __global__ void __launch_bounds__(32 * W) vjp_sym_kernel(const grav_batch b,
 					const float4* __restrict__ cp = sp + ch * 32;
 					const float4* __restrict__ cu = su + ch * 32;
 					float cax = 0.f, cay = 0.f, caz = 0.f, chx = 0.f, chy = 0.f, chz = 0.f, cg = 0.f;
-#pragma unroll 2
+					// unrolled by 4 with the forces recomputed, by 2 without (measured at 8192
+					// and 16384 bodies: 3 % faster / 1 % slower with 4 than with 2)
+#pragma unroll (FA ? 4 : 2)
 					for (int st = 0; st < 32; ++st) {
 						const float4 pj = cp[(lane + st) & 31];
 						const float4 uj = cu[(lane + st) & 31];
