@@ -165,8 +165,8 @@ class Rollout:
     components instead of 7) and the reversal v_k = v_{k+1} - T a_k uses the very a_k
     of the forward.  'auto' (default): True when that fits the slot budget
     (engine.slot_budget_bytes).  Measured on GB300 (forward + adjoint over forward,
-    uniform cube): N = 8192 -- 2.71 kept, 3.08 recomputed; N = 16384 -- 2.81 kept,
-    3.14-3.21 recomputed."""
+    uniform cube, forward fp32un): N = 8192 -- 2.75 kept, 3.07 recomputed; N = 16384 --
+    2.91 kept, 3.26 recomputed."""
 
     def __init__(self, sizes, T, steps, every=32, device=None, fwd_tile=None, tuner=None,
                  mode=None, graphs=True, adj_pairs=None, store_a='auto'):
