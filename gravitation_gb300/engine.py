@@ -478,8 +478,8 @@ class Engine:
         if code != _lib.GRAV_DEV_OK:
             self.err.zero_()
             raise _lib.GravError(_lib.GRAV_E_CUDA, 'device error flag %d (%s)' % (
-                code, 'bounded wait for a bulk copy expired' if code == _lib.GRAV_DEV_TIMEOUT
-                else 'unknown'))
+                code, 'bounded wait expired: a bulk copy or a grid barrier'
+                if code == _lib.GRAV_DEV_TIMEOUT else 'unknown'))
 
     # ---- views ----------------------------------------------------------------------
     def universe_slice(self, u):

@@ -44,7 +44,7 @@ extern "C" {
 
 /* device error flag values written by kernels into grav_batch.err */
 #define GRAV_DEV_OK 0
-#define GRAV_DEV_TIMEOUT 1    /* a bounded wait for a bulk copy expired */
+#define GRAV_DEV_TIMEOUT 1    /* a bounded device wait expired (bulk copy, grid barrier) */
 
 /* precision modes (universe_base dtype / kernel meta "precision") */
 #define GRAV_MODE_FP32 0      /* FP32 separations and weights, compensated FP32 (hi + lo) sums */

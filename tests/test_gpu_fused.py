@@ -1,8 +1,9 @@
 """GPU tests of the single-launch step (grav_step_fused) for one small universe.
 
 Each CTA holds every position in shared memory, completes its rows' accelerations and
-integrates them; a grid barrier on two device counters keeps every CTA's reads ahead of
-the writes.  Checked here, through the C ABI (Engine with fused=(threads, rows)):
+integrates them; one CTA alone, a thread-block cluster's barrier or (more than 16 CTAs)
+a grid barrier on two device counters keeps every CTA's reads ahead of the writes.
+Checked here, through the C ABI (Engine with fused=(threads, rows)):
   - the accelerations it writes (GRAV_S2_WRITE_A) against the FP64 oracle at the same
     tolerances as the two-launch step (test_gpu_parity.py), for every compiled thread
     count, rows per CTA that are and are not multiples of 32, one CTA and many;
@@ -10,7 +11,9 @@ the writes.  Checked here, through the C ABI (Engine with fused=(threads, rows))
     accelerations (_base_.py:58-62), and the refreshed stage-1 positions bit-equal to
     what grav_prepare writes from the new state;
   - agreement with the two-launch step over 20 steps, run-to-run and graph-replay
-    bit-equality, and the barrier counters back at zero after every step.
+    bit-equality, and the barrier counters back at zero after every step;
+  - the counter barrier's bounded wait: made to expire, it reports GRAV_DEV_TIMEOUT,
+    writes nothing and leaves the counters ready for the next step.
 """
 
 import ctypes
@@ -171,3 +174,30 @@ def test_fused_rejects_non_resident_grid(gpu):
     eng.set_state(*uniform_cube(64, seed=1)[:2], G_DEFAULT * uniform_cube(64, seed=1)[2])
     eng.step(2)
     eng.raise_on_device_error()
+
+
+def test_counter_barrier_timeout_is_reported(gpu):
+    """The grid barrier of a cooperative single-launch step (128 CTAs) gives up after its
+    bounded wait when the arrivals never add up -- its arrive counter is preset so far
+    below zero that nothing brings it to the grid size (a flag that nothing sets) --
+    records GRAV_DEV_TIMEOUT, writes nothing, and the last CTA out still resets the
+    counters, so the next step runs normally."""
+    n = 4096
+    eng = Engine([n], 1e3, mode='fp32', fused=(256, 32))
+    assert -(-n // 32) > 16          # more CTAs than one cluster: the counter barrier
+    r, v, m = uniform_cube(n, seed=9)
+    eng.set_state(r, v, G_DEFAULT * m)
+    r_before, v_before = eng.r.clone(), eng.v.clone()
+    eng.sync[0] = -(1 << 30)
+    eng.step(1)
+    torch.cuda.synchronize()
+    assert int(eng.err.item()) == _lib.GRAV_DEV_TIMEOUT
+    assert torch.equal(eng.r, r_before) and torch.equal(eng.v, v_before)
+    assert eng.sync.cpu().tolist() == [0, 0]
+    with pytest.raises(_lib.GravError):
+        eng.raise_on_device_error()
+    eng.err.zero_()
+    eng.step(1)
+    torch.cuda.synchronize()
+    eng.raise_on_device_error()
+    assert not torch.equal(eng.r, r_before)
