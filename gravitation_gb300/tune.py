@@ -2,15 +2,14 @@
 
 For a workload key -- the GPU (name, SM count), the precision mode, the library's
 source hash and the size bucket (single universe: N rounded up to a quarter octave,
-m * 2^k with m in 4..7;
-batch: the size classes of its universe count and of its largest universe and the
-binary order of magnitude of its sum of N^2, so that batches of the same make-up share
-a tuned tile whatever their exact sizes) -- every compiled
-tile shape, at 1, 1/2 and 1/4 of
-the resident persistent grid, is timed as full steps replayed from a CUDA graph (CUDA
-events, at least ~2 ms of steps) on a seeded synthetic state of that size, and the
-fastest is cached as JSON (the four fastest of that pass timed again, longer, and the
-best of those kept).
+m * 2^k with m in 4..7; batch: the size classes of its universe count and of its
+largest universe and the binary order of magnitude of its sum of N^2, so that batches of
+the same make-up share a tuned tile whatever their exact sizes) -- every compiled tile
+shape whose partial-sum slots fit the slot budget, at 1, 1/2 and 1/4 of the resident
+persistent grid, is timed as full steps replayed from a CUDA graph (CUDA events, at
+least ~2 ms of steps) on a seeded synthetic state of the sizes that asked, at their
+time step, and the fastest is cached as JSON (the four fastest of that pass timed
+again, longer, and the best of those kept).
 
 Cache robustness: an unreadable or malformed cache file is ignored (and rewritten),
 entries from another library build (different source hash) or naming a tile that is
@@ -51,11 +50,11 @@ def fine_class(n):
 
 def bucket_of(sizes):
     """Tuner key of a size list.  One universe: its quarter-octave class (fine_class).  A
-    batch: the size class
-    of its universe count, the binary order of magnitude of its work (sum of N^2) and
-    the size class of its largest universe, e.g. 'batch:u256:w32:max16384' -- what the
-    tile choice depends on -- so that batches drawn from one distribution (other seeds
-    of the same log-uniform range) share their tuned tile."""
+    batch: the size class of its universe count, the binary order of magnitude of its
+    work (sum of N^2) and the size class of its largest universe, e.g.
+    'batch:u256:w32:max16384' -- what the tile choice depends on -- so that batches
+    drawn from one distribution (other seeds of the same log-uniform range) share their
+    tuned tile."""
     sizes = [int(s) for s in sizes]
     if len(sizes) == 1:
         return 'single:%d' % fine_class(max(sizes[0], 1))
