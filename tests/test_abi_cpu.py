@@ -327,6 +327,11 @@ def test_fused_step_rejects_bad_calls_on_host(L):
     for m in (_lib.GRAV_MODE_FP64, _lib.GRAV_MODE_FP32U, _lib.GRAV_MODE_FP32UN,
               _lib.GRAV_MODE_FP32CU, 99):
         assert L.grav_fused_supported(m, 100, 256, 32) == 0
+    occ = ctypes.c_int32()
+    assert L.grav_fused_occupancy(f32, 100, 256, 32, None) == _lib.GRAV_E_ARG
+    assert L.grav_fused_occupancy(f32, 100, 128, 32, ctypes.byref(occ)) == _lib.GRAV_E_TILE
+    assert L.grav_fused_occupancy(_lib.GRAV_MODE_FP32U, 100, 256, 32,
+                                  ctypes.byref(occ)) == _lib.GRAV_E_TILE
     sync = ctypes.c_void_p(16)   # never dereferenced: validation fails first
     assert L.grav_step_fused(None, 1, 256, 32, sync, None) == _lib.GRAV_E_ARG
     b = _lib.Batch()
