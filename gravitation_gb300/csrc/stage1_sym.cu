@@ -402,6 +402,8 @@ static const Stage1Kernel k_table_sym[] = {
 	GRAV_SYMN_ENTRY(4, 4, 256),
 	GRAV_SYMN_ENTRY(4, 8, 256),
 	GRAV_SYMN_ENTRY(4, 2, 64),
+	GRAV_SYMN_ENTRY(8, 2, 64),
+	GRAV_SYMN_ENTRY(8, 2, 128),
 };
 
 int stage1_table_sym(const Stage1Kernel** out)
